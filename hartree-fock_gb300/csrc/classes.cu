@@ -1,0 +1,82 @@
+// Kernel instantiations and launcher of ONE shell-quartet class.  The build compiles this file once
+// per class with -DHFG_QCLASS=<0..20>, so the 21 classes compile in parallel.
+#include "engine.h"
+
+#ifndef HFG_QCLASS
+#error "compile with -DHFG_QCLASS=<quartet class>"
+#endif
+
+namespace hfg
+{
+namespace
+{
+constexpr int QC = HFG_QCLASS;
+constexpr int bra_class()
+{
+    int p = 0;
+    while ((p + 1) * (p + 2) / 2 <= QC) ++p;
+    return p;
+}
+constexpr int P1 = bra_class();
+constexpr int P2 = QC - P1 * (P1 + 1) / 2;
+constexpr int LA = pair_class_l1(P1), LB = pair_class_l2(P1), LC = pair_class_l1(P2), LD = pair_class_l2(P2);
+constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
+constexpr int L   = LA + LB + LC + LD;
+// Thread-per-quartet when the quartet's register arrays (integrals, G, R) stay small.
+constexpr bool kWarp = (NAB * NCD + nherm(LA + LB) * NCD + nherm(L)) > 128;
+
+template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
+{
+    if (c.count_host == 0)
+        return cudaSuccess;
+    const size_t slice_bytes = sizeof(Real) * BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow;
+    if constexpr (kWarp)
+    {
+        using W             = WarpLayout<LA, LB, LC, LD, Real>;
+        const size_t smem   = slice_bytes + sizeof(Real) * W::kPerWarp * kWarpKernelWarps;
+        auto kern           = jk_class_warp_kernel<LA, LB, LC, LD, Real, UHF>;
+        cudaError_t e       = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess)
+            return e;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kWarpKernelWarps, smem);
+        if (e != cudaSuccess)
+            return e;
+        const unsigned long long need = (c.count_host + kWarpKernelWarps - 1) / kWarpKernelWarps;
+        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+        const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
+        kern<<<grid, 32 * kWarpKernelWarps, smem, c.stream>>>(c.list, c.count_dev, c.view,
+                                                              static_cast<const Real*>(c.boys_slice), c.tables);
+    }
+    else
+    {
+        auto kern           = jk_class_kernel<LA, LB, LC, LD, Real, UHF>;
+        const size_t smem   = slice_bytes;
+        cudaError_t e       = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess)
+            return e;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+        if (e != cudaSuccess)
+            return e;
+        const unsigned long long need = (c.count_host + 127) / 128;
+        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+        const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
+        kern<<<grid, 128, smem, c.stream>>>(c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
+    }
+    return cudaGetLastError();
+}
+} // namespace
+
+#define HFG_CAT2(a, b) a##b
+#define HFG_CAT(a, b) HFG_CAT2(a, b)
+
+cudaError_t HFG_CAT(launch_class_, HFG_QCLASS)(const ClassLaunch& c)
+{
+    if (c.fp32)
+        return c.uhf ? launch_t<float, true>(c) : launch_t<float, false>(c);
+    return c.uhf ? launch_t<double, true>(c) : launch_t<double, false>(c);
+}
+
+bool HFG_CAT(class_uses_warp_, HFG_QCLASS)() { return kWarp; }
+} // namespace hfg

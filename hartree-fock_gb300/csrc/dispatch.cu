@@ -1,0 +1,34 @@
+// Table of the per-class launchers (one translation unit per class, see classes.cu).
+#include "engine.h"
+
+namespace hfg
+{
+#define HFG_DECL(c)                                                                                                    \
+    cudaError_t launch_class_##c(const ClassLaunch&);                                                                 \
+    bool class_uses_warp_##c();
+HFG_DECL(0) HFG_DECL(1) HFG_DECL(2) HFG_DECL(3) HFG_DECL(4) HFG_DECL(5) HFG_DECL(6) HFG_DECL(7) HFG_DECL(8)
+HFG_DECL(9) HFG_DECL(10) HFG_DECL(11) HFG_DECL(12) HFG_DECL(13) HFG_DECL(14) HFG_DECL(15) HFG_DECL(16)
+HFG_DECL(17) HFG_DECL(18) HFG_DECL(19) HFG_DECL(20)
+#undef HFG_DECL
+
+static const ClassLauncher kLaunch[kNumQuartetClasses] = {
+    launch_class_0,  launch_class_1,  launch_class_2,  launch_class_3,  launch_class_4,  launch_class_5,
+    launch_class_6,  launch_class_7,  launch_class_8,  launch_class_9,  launch_class_10, launch_class_11,
+    launch_class_12, launch_class_13, launch_class_14, launch_class_15, launch_class_16, launch_class_17,
+    launch_class_18, launch_class_19, launch_class_20};
+static bool (*const kWarp[kNumQuartetClasses])() = {
+    class_uses_warp_0,  class_uses_warp_1,  class_uses_warp_2,  class_uses_warp_3,  class_uses_warp_4,
+    class_uses_warp_5,  class_uses_warp_6,  class_uses_warp_7,  class_uses_warp_8,  class_uses_warp_9,
+    class_uses_warp_10, class_uses_warp_11, class_uses_warp_12, class_uses_warp_13, class_uses_warp_14,
+    class_uses_warp_15, class_uses_warp_16, class_uses_warp_17, class_uses_warp_18, class_uses_warp_19,
+    class_uses_warp_20};
+
+cudaError_t launch_class(int qclass, const ClassLaunch& L)
+{
+    if (qclass < 0 || qclass >= kNumQuartetClasses)
+        return cudaErrorInvalidValue;
+    return kLaunch[qclass](L);
+}
+
+bool class_uses_warp_kernel(int qclass) { return qclass >= 0 && qclass < kNumQuartetClasses && kWarp[qclass](); }
+} // namespace hfg

@@ -1,0 +1,1191 @@
+// hfgpu engine: basis packing, Schwartz screening, device quartet lists, class dispatch and the C ABI.
+//
+// Reference counterparts (MalachiF1/Hartree-Fock):
+//   IntegralEngine::IntegralEngine          src/IntegralEngine.cpp:13-75    -> hfg_create / pack_molecules
+//   computePrimitivePairData/HermiteCoeffs  src/IntegralEngine.cpp:995-1079 -> build_pair_tables (once per engine)
+//   schwartzScreeningMatrix                 src/IntegralEngine.cpp:695-728  -> compute_schwartz
+//   SCF::buildFockMatrixDirect              src/SCF.cpp:523-744             -> fock_direct
+//
+// Device data layout (HBM):
+//   pairs_      PairRec per shell pair (a >= b within a molecule), oriented so l(sh1) >= l(sh2)
+//   pptab64_/32 per pair class, primitive-pair records of pp_stride(l1,l2) values: 1/p, p, P, Kw, E3
+//   cls_*       per pair class, pair ids sorted by (molecule, Q descending), with their Q values
+//   lists       per quartet class and precision, the surviving quartets (bra pair, ket pair)
+//   matrices    per molecule n x n column-major blocks, concatenated (dD, X, Y, J, K)
+#include "engine.h"
+#include "hfgpu.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace hfg
+{
+namespace
+{
+thread_local std::string g_create_error;
+
+struct HfgError : std::runtime_error
+{
+    int code;
+    HfgError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define HFG_CUDA(call)                                                                                               \
+    do                                                                                                               \
+    {                                                                                                                \
+        cudaError_t e_ = (call);                                                                                     \
+        if (e_ != cudaSuccess)                                                                                       \
+            throw HfgError(e_ == cudaErrorMemoryAllocation ? HFG_ERR_NOMEM : HFG_ERR_CUDA,                           \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                                      \
+    } while (0)
+
+template <typename T> struct DevBuf
+{
+    T* p     = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count)
+    {
+        if (count <= n && p)
+            return;
+        release();
+        if (count == 0)
+            return;
+        HFG_CUDA(cudaMalloc(&p, sizeof(T) * count));
+        n = count;
+    }
+    void upload(const std::vector<T>& v, cudaStream_t s)
+    {
+        alloc(v.size());
+        if (!v.empty())
+            HFG_CUDA(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+    }
+};
+
+struct MolInfo
+{
+    int nshells, nao;
+    int sh_off;         // first global shell
+    long long mat_off;  // offset of its n x n block
+    long long smax_off; // offset of its nshells x nshells shell-max block
+};
+
+// Host-side basis of one molecule (copied from the caller).
+struct HostBasis
+{
+    std::vector<int> l, nprim, prim_off, ao_off;
+    std::vector<double> centers, alpha, coeff, radial; // radial: coeff-free radial norm per primitive
+};
+} // namespace
+} // namespace hfg
+
+struct hfg_engine
+{
+    int device  = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] {};
+    std::string last_error;
+
+    int nmol = 0;
+    std::vector<hfg::MolInfo> mols;
+    std::vector<hfg::HostBasis> basis;
+    long long mat_total  = 0; // sum n_m^2
+    long long smax_total = 0; // sum nshells_m^2
+    int nshells_total    = 0;
+
+    std::vector<hfg::PairRec> pairs;
+    std::vector<int> pair_class_of;
+    hfg::DevBuf<hfg::PairRec> d_pairs;
+    hfg::DevBuf<double> d_pptab64[hfg::kNumPairClasses];
+    hfg::DevBuf<float> d_pptab32[hfg::kNumPairClasses];
+    hfg::DevBuf<long long> d_mat_off;
+    hfg::DevBuf<int> d_mat_ld;
+    hfg::DevBuf<long long> d_smax_off; // per molecule offset of its shell-max block
+    hfg::DevBuf<int> d_nsh;            // per molecule shell count
+    hfg::DevBuf<int> d_shnao;          // per pair: Cartesian counts of sh1, sh2
+    hfg::DevBuf<hfg::WarpTables> d_tables;
+    hfg::DevBuf<double> d_boys64[hfg::kMaxLt + 1];
+    hfg::DevBuf<float> d_boys32[hfg::kMaxLt + 1];
+
+    // Schwartz bounds per pair, and per pair class sorted lists.
+    std::vector<double> Qpair;
+    bool have_Q = false;
+    std::vector<int> cls_ids[hfg::kNumPairClasses];
+    std::vector<double> cls_Q[hfg::kNumPairClasses];
+    std::vector<int2> cls_rng[hfg::kNumPairClasses]; // per molecule [begin, end) in the class list
+    hfg::DevBuf<int> d_cls_ids[hfg::kNumPairClasses];
+    hfg::DevBuf<double> d_cls_Q[hfg::kNumPairClasses];
+    hfg::DevBuf<int2> d_cls_rng[hfg::kNumPairClasses];
+
+    // Quartet lists (capacity for the Schwartz threshold they were sized for).
+    double cap_thr = -1.0;
+    unsigned long long cap[hfg::kNumQuartetClasses] {};
+    bool cap_mixed = false;
+    hfg::DevBuf<hfg::Quartet> d_list[hfg::kNumQuartetClasses][2];
+    hfg::DevBuf<unsigned long long> d_counts; // [qclass][prec] quartets, then [qclass][prec] prim quartets, then overflow
+    std::vector<unsigned long long> h_counts;
+
+    // Work matrices.
+    hfg::DevBuf<double> d_dD[3];   // tot, alpha, beta (FP64)
+    hfg::DevBuf<float> d_dDf[3];   // FP32 copies for the FP32 kernels
+    hfg::DevBuf<double> d_acc[3];  // X, Ya, Yb
+    hfg::DevBuf<double> d_out[3];  // J, Ka, Kb
+    hfg::DevBuf<double> d_smax[3]; // shell-pair maxima of |dD|
+    hfg::DevBuf<double> d_store;
+    hfg::DevBuf<hfg::Quartet> d_tmp_list;
+    hfg::DevBuf<unsigned long long> d_tmp_count;
+
+    bool last_valid = false;
+    int last_mixed  = 0;
+};
+
+namespace hfg
+{
+namespace
+{
+// ------------------------------------------------------------------------------------------------
+// Small kernels.
+// ------------------------------------------------------------------------------------------------
+__global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = static_cast<float>(a[i]);
+}
+
+// Shell-pair maxima of |dD| (SCF.cpp:544-575) for every molecule block.
+__global__ void shell_max_kernel(const double* __restrict__ dD, const PairRec* __restrict__ pairs, int npairs,
+                                 const long long* __restrict__ mat_off, const int* __restrict__ mat_ld,
+                                 const long long* __restrict__ smax_off, const int* __restrict__ nsh,
+                                 const int* __restrict__ sh_nao, double* __restrict__ M)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x)
+    {
+        const PairRec pr = pairs[k];
+        const long long off = mat_off[pr.mol];
+        const int n = mat_ld[pr.mol], ns = nsh[pr.mol];
+        const int n1 = sh_nao[k * 2], n2 = sh_nao[k * 2 + 1];
+        double mx = 0.0;
+        for (int j = 0; j < n2; ++j)
+            for (int i = 0; i < n1; ++i) mx = fmax(mx, fabs(dD[off + (pr.ao1 + i) + (long long)(pr.ao2 + j) * n]));
+        M[smax_off[pr.mol] + pr.sh1 + (long long)pr.sh2 * ns] = mx;
+        M[smax_off[pr.mol] + pr.sh2 + (long long)pr.sh1 * ns] = mx;
+    }
+}
+
+struct BuildArgs
+{
+    const int* ids1;
+    const double* Q1;
+    int n1;
+    const int* ids2;
+    const double* Q2;
+    const int2* rng2;
+    bool same_class;
+    const PairRec* pairs;
+    const double* Mt;
+    const double* Ma;
+    const double* Mb; // null for RHF
+    const long long* smax_off;
+    const int* nsh;
+    double sthr, dthr, cutoff;
+    int mixed;
+    Quartet* out64;
+    Quartet* out32;
+    unsigned long long cap;
+    unsigned long long* cnt64;
+    unsigned long long* cnt32;
+    unsigned long long* prim64;
+    unsigned long long* prim32;
+    unsigned long long* overflow;
+};
+
+// Survival list of one quartet class: one warp per bra pair; candidate ket pairs are the Schwartz
+// prefix of the ket class list (sorted by Q descending, so Q_i*Q_j < thr holds from a point on), then
+// the density predicate of SCF.cpp:610-623.  FP32 / FP64 split by the quartet bound Q_i Q_j max|dD|.
+__global__ void build_lists_kernel(BuildArgs a)
+{
+    const int lane = threadIdx.x & 31;
+    const int i    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= a.n1)
+        return;
+    const int pid_i  = a.ids1[i];
+    const double Qi  = a.Q1[i];
+    const PairRec pi = a.pairs[pid_i];
+    const int2 r     = a.rng2[pi.mol];
+    const int jb     = r.x;
+    const int je     = a.same_class ? i + 1 : r.y;
+    int lo = jb, hi = je;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi) >> 1;
+        if (Qi * a.Q2[mid] < a.sthr)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    const int jend = lo;
+    const long long so = a.smax_off[pi.mol];
+    const int ns = a.nsh[pi.mol];
+    auto M = [&](const double* m, int x, int y) { return m[so + x + (long long)y * ns]; };
+    const int sa = pi.sh1, sb = pi.sh2;
+    const double dab = 2.0 * M(a.Mt, sa, sb);
+    for (int base = jb; base < jend; base += 32)
+    {
+        const int j = base + lane;
+        bool s64 = false, s32 = false;
+        int pid_j = 0;
+        unsigned long long prims = 0;
+        if (j < jend)
+        {
+            pid_j = a.ids2[j];
+            const PairRec pj = a.pairs[pid_j];
+            const int sc = pj.sh1, sd = pj.sh2;
+            double md = fmax(fmax(dab, 2.0 * M(a.Mt, sc, sd)),
+                             fmax(fmax(M(a.Ma, sa, sc), M(a.Ma, sa, sd)), fmax(M(a.Ma, sb, sc), M(a.Ma, sb, sd))));
+            if (a.Mb)
+                md = fmax(md, fmax(fmax(M(a.Mb, sa, sc), M(a.Mb, sa, sd)), fmax(M(a.Mb, sb, sc), M(a.Mb, sb, sd))));
+            if (md >= a.dthr)
+            {
+                const bool lowp = a.mixed && (Qi * a.Q2[j] * md < a.cutoff);
+                s32 = lowp;
+                s64 = !lowp;
+                prims = (unsigned long long)pi.npp * pj.npp;
+            }
+        }
+        for (int prec = 0; prec < 2; ++prec)
+        {
+            const bool mine = prec == 0 ? s64 : s32;
+            const unsigned mask = __ballot_sync(0xffffffffu, mine);
+            if (mask == 0)
+                continue;
+            unsigned long long* cnt = prec == 0 ? a.cnt64 : a.cnt32;
+            unsigned long long slot = 0;
+            const int leader = __ffs(mask) - 1;
+            if (lane == leader)
+                slot = atomicAdd(cnt, (unsigned long long)__popc(mask));
+            slot = __shfl_sync(0xffffffffu, slot, leader);
+            unsigned long long pr = mine ? prims : 0ull;
+            for (int o = 16; o > 0; o >>= 1) pr += __shfl_down_sync(0xffffffffu, pr, o);
+            if (lane == 0)
+                atomicAdd(prec == 0 ? a.prim64 : a.prim32, pr);
+            if (mine)
+            {
+                const unsigned long long pos = slot + __popc(mask & ((1u << lane) - 1u));
+                Quartet* out = prec == 0 ? a.out64 : a.out32;
+                if (pos < a.cap)
+                    out[pos] = Quartet {static_cast<uint32_t>(pid_i), static_cast<uint32_t>(pid_j)};
+                else
+                    atomicAdd(a.overflow, 1ull);
+            }
+        }
+    }
+}
+
+// J = X + X^T, K = Y + Y^T over the concatenated molecule blocks.
+__global__ void symmetrize_kernel(const double* __restrict__ X, double* __restrict__ J, const long long* __restrict__ mat_off,
+                                  const int* __restrict__ mat_ld, int nmol, long long total)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x)
+    {
+        int lo = 0, hi = nmol - 1;
+        while (lo < hi)
+        {
+            const int mid = (lo + hi + 1) >> 1;
+            if (mat_off[mid] <= e)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const long long off = mat_off[lo];
+        const int n = mat_ld[lo];
+        const long long loc = e - off;
+        const int r = static_cast<int>(loc % n), c = static_cast<int>(loc / n);
+        J[e] = X[e] + X[off + c + (long long)r * n];
+    }
+}
+
+// Q(pair) = sqrt(max_ij (ij|ij)) from stored (P|P) blocks.
+__global__ void schwartz_from_store_kernel(const double* __restrict__ store, const Quartet* __restrict__ list, int n,
+                                           int nab, double* __restrict__ Qpair)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    {
+        double mx = 0.0;
+        for (int ij = 0; ij < nab; ++ij) mx = fmax(mx, store[(long long)k * nab * nab + ij * nab + ij]);
+        Qpair[list[k].bra] = sqrt(mx);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host helpers.
+// ------------------------------------------------------------------------------------------------
+inline int grid_for(long long n, int threads, int num_sms)
+{
+    long long g = (n + threads - 1) / threads;
+    const long long cap = static_cast<long long>(num_sms) * 16;
+    if (g > cap)
+        g = cap;
+    return static_cast<int>(g < 1 ? 1 : g);
+}
+
+double ang_norm_host(int l, int c)
+{
+    const int i = cart_exp(l, c, 0), j = cart_exp(l, c, 1), k = cart_exp(l, c, 2);
+    return 1.0 / std::sqrt(static_cast<double>(dfact_odd(2 * i - 1) * dfact_odd(2 * j - 1) * dfact_odd(2 * k - 1)));
+}
+
+void validate_and_copy(const hfg_basis& b, HostBasis& hb)
+{
+    if (b.nshells <= 0 || b.nao <= 0 || b.nprim <= 0 || !b.l || !b.nprim_sh || !b.prim_off || !b.ao_off ||
+        !b.norm_off || !b.centers || !b.alpha || !b.coeff || !b.norms || !b.am)
+        throw HfgError(HFG_ERR_INVALID, "basis: missing arrays or empty basis");
+    hb.l.assign(b.l, b.l + b.nshells);
+    hb.nprim.assign(b.nprim_sh, b.nprim_sh + b.nshells);
+    hb.prim_off.assign(b.prim_off, b.prim_off + b.nshells);
+    hb.ao_off.assign(b.ao_off, b.ao_off + b.nshells);
+    hb.centers.assign(b.centers, b.centers + 3 * b.nshells);
+    hb.alpha.assign(b.alpha, b.alpha + b.nprim);
+    hb.coeff.assign(b.coeff, b.coeff + b.nprim);
+    hb.radial.assign(b.nprim, 0.0);
+    int ao = 0;
+    for (int s = 0; s < b.nshells; ++s)
+    {
+        const int l = b.l[s];
+        if (l < 0 || l > kMaxL)
+            throw HfgError(HFG_ERR_UNSUPPORTED, "basis: angular momentum " + std::to_string(l) +
+                                                    " above d (l <= 2) is not supported");
+        if (b.nprim_sh[s] <= 0 || b.prim_off[s] < 0 || b.prim_off[s] + b.nprim_sh[s] > b.nprim)
+            throw HfgError(HFG_ERR_BASIS, "basis: bad primitive range of shell " + std::to_string(s));
+        if (b.ao_off[s] != ao)
+            throw HfgError(HFG_ERR_BASIS, "basis: AO offsets are not contiguous at shell " + std::to_string(s));
+        const int nc = ncart(l);
+        for (int c = 0; c < nc; ++c)
+            for (int ax = 0; ax < 3; ++ax)
+                if (b.am[3 * (ao + c) + ax] != cart_exp(l, c, ax))
+                    throw HfgError(HFG_ERR_BASIS, "basis: Cartesian order differs from the reference's at shell " +
+                                                      std::to_string(s));
+        for (int p = 0; p < b.nprim_sh[s]; ++p)
+        {
+            const double a = b.alpha[b.prim_off[s] + p];
+            if (!(a > 0.0) || !std::isfinite(a) || !std::isfinite(b.coeff[b.prim_off[s] + p]))
+                throw HfgError(HFG_ERR_BASIS, "basis: non-positive or non-finite exponent in shell " + std::to_string(s));
+            // The reference's factor (src/Basis.cpp:69-73) is radial(alpha, l) * angular(component).
+            const double rad = b.norms[b.norm_off[s] + p * nc + 0] / ang_norm_host(l, 0);
+            for (int c = 0; c < nc; ++c)
+            {
+                const double want = rad * ang_norm_host(l, c);
+                const double got  = b.norms[b.norm_off[s] + p * nc + c];
+                if (!(std::fabs(got - want) <= 1e-12 * std::fabs(want)))
+                    throw HfgError(HFG_ERR_BASIS, "basis: normalisation factors of shell " + std::to_string(s) +
+                                                      " do not factor into radial x angular parts");
+            }
+            hb.radial[b.prim_off[s] + p] = rad;
+        }
+        for (int ax = 0; ax < 3; ++ax)
+            if (!std::isfinite(b.centers[3 * s + ax]))
+                throw HfgError(HFG_ERR_BASIS, "basis: non-finite centre of shell " + std::to_string(s));
+        ao += nc;
+    }
+    if (ao != b.nao)
+        throw HfgError(HFG_ERR_BASIS, "basis: nao does not match the shells");
+}
+
+// 1-D Hermite coefficients E^{ij}_t of one axis for i <= l1, j <= l2 (McMurchie-Davidson recurrences;
+// the reference builds the same table in src/IntegralEngine.cpp:1025-1079).  E[i][j][t], K not included.
+void hermite_1d(int l1, int l2, double p, double PA, double PB, double E[kMaxL + 1][kMaxL + 1][2 * kMaxL + 1])
+{
+    std::memset(E, 0, sizeof(double) * (kMaxL + 1) * (kMaxL + 1) * (2 * kMaxL + 1));
+    const double h = 0.5 / p;
+    E[0][0][0]     = 1.0;
+    for (int i = 0; i <= l1; ++i)
+        for (int j = 0; j <= l2; ++j)
+        {
+            if (i == 0 && j == 0)
+                continue;
+            const bool up_i = i > 0;
+            const int pi = up_i ? i - 1 : i, pj = up_i ? j : j - 1;
+            const double X = up_i ? PA : PB;
+            for (int t = 0; t <= i + j; ++t)
+            {
+                double v = 0.0;
+                if (t <= pi + pj)
+                    v += X * E[pi][pj][t];
+                if (t >= 1)
+                    v += h * E[pi][pj][t - 1];
+                if (t + 1 <= pi + pj)
+                    v += (t + 1) * E[pi][pj][t + 1];
+                E[i][j][t] = v;
+            }
+        }
+}
+} // namespace
+
+// Builds pairs, primitive-pair tables and sorted class lists skeleton (without Q).
+static void pack_molecules(hfg_engine* e)
+{
+    using namespace hfg;
+    std::vector<std::vector<double>> tab(kNumPairClasses);
+    std::vector<int> class_npp(kNumPairClasses, 0);
+    for (int m = 0; m < e->nmol; ++m)
+    {
+        const HostBasis& b = e->basis[m];
+        const int ns       = e->mols[m].nshells;
+        for (int s1 = 0; s1 < ns; ++s1)
+            for (int s2 = 0; s2 <= s1; ++s2)
+            {
+                int a = s1, bb = s2;
+                if (b.l[bb] > b.l[a])
+                    std::swap(a, bb);
+                const int l1 = b.l[a], l2 = b.l[bb];
+                const int pc = pair_class(l1, l2);
+                PairRec pr {};
+                pr.sh1    = a;
+                pr.sh2    = bb;
+                pr.ao1    = b.ao_off[a];
+                pr.ao2    = b.ao_off[bb];
+                pr.pp_off = class_npp[pc];
+                pr.npp    = b.nprim[a] * b.nprim[bb];
+                pr.mol    = m;
+                pr.same   = (s1 == s2) ? 1 : 0;
+                const double* A = &b.centers[3 * a];
+                const double* B = &b.centers[3 * bb];
+                const double AB2 = (A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) + (A[2] - B[2]) * (A[2] - B[2]);
+                const int stride = pp_stride(l1, l2);
+                for (int pa = 0; pa < b.nprim[a]; ++pa)
+                    for (int pb = 0; pb < b.nprim[bb]; ++pb)
+                    {
+                        const double aa = b.alpha[b.prim_off[a] + pa], ab = b.alpha[b.prim_off[bb] + pb];
+                        const double p = aa + ab, ip = 1.0 / p;
+                        double P[3], PA[3], PB[3];
+                        for (int k = 0; k < 3; ++k)
+                        {
+                            P[k]  = (aa * A[k] + ab * B[k]) * ip;
+                            PA[k] = P[k] - A[k];
+                            PB[k] = P[k] - B[k];
+                        }
+                        const double Kw = std::exp(-aa * ab * ip * AB2) * b.coeff[b.prim_off[a] + pa] *
+                                          b.coeff[b.prim_off[bb] + pb] * b.radial[b.prim_off[a] + pa] *
+                                          b.radial[b.prim_off[bb] + pb];
+                        std::vector<double> rec(stride, 0.0);
+                        rec[0] = ip;
+                        rec[1] = p;
+                        rec[2] = P[0];
+                        rec[3] = P[1];
+                        rec[4] = P[2];
+                        rec[5] = Kw;
+                        double E[3][kMaxL + 1][kMaxL + 1][2 * kMaxL + 1];
+                        for (int k = 0; k < 3; ++k) hermite_1d(l1, l2, p, PA[k], PB[k], E[k]);
+                        int x = kPairHeader;
+                        for (int ij = 0; ij < ncart(l1) * ncart(l2); ++ij)
+                        {
+                            const int ci = ij / ncart(l2), cj = ij % ncart(l2);
+                            const int ix = cart_exp(l1, ci, 0), iy = cart_exp(l1, ci, 1), iz = cart_exp(l1, ci, 2);
+                            const int jx = cart_exp(l2, cj, 0), jy = cart_exp(l2, cj, 1), jz = cart_exp(l2, cj, 2);
+                            for (int v = 0; v <= iz + jz; ++v)
+                                for (int u = 0; u <= iy + jy; ++u)
+                                    for (int t = 0; t <= ix + jx; ++t)
+                                        rec[x++] = E[0][ix][jx][t] * E[1][iy][jy][u] * E[2][iz][jz][v];
+                        }
+                        tab[pc].insert(tab[pc].end(), rec.begin(), rec.end());
+                    }
+                class_npp[pc] += pr.npp;
+                e->pairs.push_back(pr);
+                e->pair_class_of.push_back(pc);
+            }
+    }
+    e->d_pairs.upload(e->pairs, e->stream);
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        e->d_pptab64[pc].upload(tab[pc], e->stream);
+        std::vector<float> f(tab[pc].begin(), tab[pc].end());
+        e->d_pptab32[pc].upload(f, e->stream);
+    }
+    std::vector<long long> moff;
+    std::vector<int> mld;
+    for (const auto& mi : e->mols)
+    {
+        moff.push_back(mi.mat_off);
+        mld.push_back(mi.nao);
+    }
+    e->d_mat_off.upload(moff, e->stream);
+    e->d_mat_ld.upload(mld, e->stream);
+    {
+        std::vector<long long> so;
+        std::vector<int> nsh;
+        for (const auto& mi : e->mols)
+        {
+            so.push_back(mi.smax_off);
+            nsh.push_back(mi.nshells);
+        }
+        std::vector<int> shnao(2 * e->pairs.size());
+        for (size_t k = 0; k < e->pairs.size(); ++k)
+        {
+            const auto& b = e->basis[e->pairs[k].mol];
+            shnao[2 * k]     = ncart(b.l[e->pairs[k].sh1]);
+            shnao[2 * k + 1] = ncart(b.l[e->pairs[k].sh2]);
+        }
+        e->d_smax_off.upload(so, e->stream);
+        e->d_nsh.upload(nsh, e->stream);
+        e->d_shnao.upload(shnao, e->stream);
+    }
+    auto tables = std::make_unique<WarpTables>();
+    build_warp_tables(*tables);
+    e->d_tables.alloc(1);
+    HFG_CUDA(cudaMemcpyAsync(e->d_tables.p, tables.get(), sizeof(WarpTables), cudaMemcpyHostToDevice, e->stream));
+    for (int L = 0; L <= kMaxLt; ++L)
+    {
+        e->d_boys64[L].upload(boys_slice_host<double>(L), e->stream);
+        e->d_boys32[L].upload(boys_slice_host<float>(L), e->stream);
+    }
+    HFG_CUDA(cudaStreamSynchronize(e->stream));
+}
+
+static FockView base_view(hfg_engine* e, bool fp32)
+{
+    FockView v {};
+    v.pairs = e->d_pairs.p;
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+        v.pptab[pc] = fp32 ? static_cast<const void*>(e->d_pptab32[pc].p) : static_cast<const void*>(e->d_pptab64[pc].p);
+    v.mat_off = e->d_mat_off.p;
+    v.mat_ld  = e->d_mat_ld.p;
+    return v;
+}
+
+static int qclass_of(int pb, int pk) { return quartet_class(std::max(pb, pk), std::min(pb, pk)); }
+
+// Evaluates a list of quartets of one class in store mode (FP64) into d_store.
+static void eval_store(hfg_engine* e, int qc, const std::vector<Quartet>& q)
+{
+    const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+    const int P2 = qc - P1 * (P1 + 1) / 2;
+    const int nq = ncart(pair_class_l1(P1)) * ncart(pair_class_l2(P1)) * ncart(pair_class_l1(P2)) * ncart(pair_class_l2(P2));
+    e->d_tmp_list.upload(q, e->stream);
+    e->d_tmp_count.alloc(1);
+    unsigned long long n = q.size();
+    HFG_CUDA(cudaMemcpyAsync(e->d_tmp_count.p, &n, sizeof(n), cudaMemcpyHostToDevice, e->stream));
+    e->d_store.alloc(q.size() * nq);
+    ClassLaunch L {};
+    L.list       = e->d_tmp_list.p;
+    L.count_dev  = e->d_tmp_count.p;
+    L.count_host = n;
+    L.view       = base_view(e, false);
+    L.view.store = e->d_store.p;
+    L.view.ao_thr = 0.0;
+    L.boys_slice = e->d_boys64[pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2)].p;
+    L.tables     = e->d_tables.p;
+    L.fp32       = false;
+    L.uhf        = false;
+    L.stream     = e->stream;
+    L.num_sms    = e->num_sms;
+    HFG_CUDA(launch_class(qc, L));
+}
+
+static void compute_schwartz(hfg_engine* e)
+{
+    e->Qpair.assign(e->pairs.size(), 0.0);
+    DevBuf<double> dQ;
+    dQ.alloc(e->pairs.size());
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        std::vector<Quartet> q;
+        for (size_t k = 0; k < e->pairs.size(); ++k)
+            if (e->pair_class_of[k] == pc)
+                q.push_back(Quartet {static_cast<uint32_t>(k), static_cast<uint32_t>(k)});
+        if (q.empty())
+            continue;
+        eval_store(e, quartet_class(pc, pc), q);
+        const int nab = ncart(pair_class_l1(pc)) * ncart(pair_class_l2(pc));
+        schwartz_from_store_kernel<<<grid_for(q.size(), 128, e->num_sms), 128, 0, e->stream>>>(
+            e->d_store.p, e->d_tmp_list.p, static_cast<int>(q.size()), nab, dQ.p);
+        HFG_CUDA(cudaGetLastError());
+        HFG_CUDA(cudaStreamSynchronize(e->stream));
+    }
+    HFG_CUDA(cudaMemcpyAsync(e->Qpair.data(), dQ.p, sizeof(double) * e->pairs.size(), cudaMemcpyDeviceToHost, e->stream));
+    HFG_CUDA(cudaStreamSynchronize(e->stream));
+    e->d_store.release();
+}
+
+// Sorts each pair class by (molecule, Q descending) and uploads the class lists.
+static void sort_classes(hfg_engine* e)
+{
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        auto& ids = e->cls_ids[pc];
+        ids.clear();
+        for (size_t k = 0; k < e->pairs.size(); ++k)
+            if (e->pair_class_of[k] == pc)
+                ids.push_back(static_cast<int>(k));
+        std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
+            if (e->pairs[x].mol != e->pairs[y].mol)
+                return e->pairs[x].mol < e->pairs[y].mol;
+            return e->Qpair[x] > e->Qpair[y];
+        });
+        e->cls_Q[pc].resize(ids.size());
+        for (size_t k = 0; k < ids.size(); ++k) e->cls_Q[pc][k] = e->Qpair[ids[k]];
+        e->cls_rng[pc].assign(e->nmol, make_int2(0, 0));
+        size_t k = 0;
+        for (int m = 0; m < e->nmol; ++m)
+        {
+            const size_t b = k;
+            while (k < ids.size() && e->pairs[ids[k]].mol == m) ++k;
+            e->cls_rng[pc][m] = make_int2(static_cast<int>(b), static_cast<int>(k));
+        }
+        e->d_cls_ids[pc].upload(ids, e->stream);
+        e->d_cls_Q[pc].upload(e->cls_Q[pc], e->stream);
+        e->d_cls_rng[pc].upload(e->cls_rng[pc], e->stream);
+    }
+    HFG_CUDA(cudaStreamSynchronize(e->stream));
+    e->have_Q  = true;
+    e->cap_thr = -1.0; // capacities depend on Q
+}
+
+// Exact Schwartz-only survivor count per quartet class (an upper bound of any build's list).
+static void size_lists(hfg_engine* e, double sthr, bool mixed)
+{
+    if (e->cap_thr == sthr && (!mixed || e->cap_mixed))
+        return;
+    for (int P1 = 0; P1 < kNumPairClasses; ++P1)
+        for (int P2 = 0; P2 <= P1; ++P2)
+        {
+            const int qc = quartet_class(P1, P2);
+            unsigned long long c = 0;
+            const auto& Q1 = e->cls_Q[P1];
+            const auto& Q2 = e->cls_Q[P2];
+            for (size_t i = 0; i < Q1.size(); ++i)
+            {
+                const int mol = e->pairs[e->cls_ids[P1][i]].mol;
+                const int jb = e->cls_rng[P2][mol].x;
+                const int je = (P1 == P2) ? static_cast<int>(i) + 1 : e->cls_rng[P2][mol].y;
+                int lo = jb, hi = je;
+                while (lo < hi)
+                {
+                    const int mid = (lo + hi) >> 1;
+                    if (Q1[i] * Q2[mid] < sthr)
+                        hi = mid;
+                    else
+                        lo = mid + 1;
+                }
+                c += static_cast<unsigned long long>(lo - jb);
+            }
+            e->cap[qc] = c;
+            e->d_list[qc][0].alloc(std::max<unsigned long long>(c, 1));
+            if (mixed)
+                e->d_list[qc][1].alloc(std::max<unsigned long long>(c, 1));
+        }
+    e->cap_thr   = sthr;
+    e->cap_mixed = mixed;
+}
+
+static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats* st)
+{
+    if (!(r.schwartz_threshold >= 0.0) || !(r.density_threshold >= 0.0) || !std::isfinite(r.schwartz_threshold) ||
+        !std::isfinite(r.density_threshold))
+        throw HfgError(HFG_ERR_INVALID, "fock: thresholds must be finite and >= 0");
+    if (!r.dD_tot || !r.dD_alpha || !r.J || !r.K_alpha || (r.unrestricted && (!r.dD_beta || !r.K_beta)))
+        throw HfgError(HFG_ERR_INVALID, "fock: missing matrix pointer");
+    if (r.precision != HFG_PRECISION_FP64 && r.precision != HFG_PRECISION_MIXED)
+        throw HfgError(HFG_ERR_INVALID, "fock: unknown precision mode");
+    const bool mixed = r.precision == HFG_PRECISION_MIXED;
+    const bool uhf   = r.unrestricted != 0;
+    if (!e->have_Q)
+    {
+        compute_schwartz(e);
+        sort_classes(e);
+    }
+    size_lists(e, r.schwartz_threshold, mixed);
+    const long long N2 = e->mat_total;
+    cudaStream_t s     = e->stream;
+    const int nspin    = uhf ? 3 : 2;
+    const double* src[3] = {r.dD_tot, r.dD_alpha, r.dD_beta};
+    for (int k = 0; k < 3; ++k)
+    {
+        e->d_dD[k].alloc(N2);
+        e->d_acc[k].alloc(N2);
+        e->d_out[k].alloc(N2);
+        e->d_smax[k].alloc(e->smax_total);
+        if (mixed)
+            e->d_dDf[k].alloc(N2);
+    }
+    HFG_CUDA(cudaEventRecord(e->ev[0], s));
+    for (int k = 0; k < nspin; ++k)
+    {
+        HFG_CUDA(cudaMemcpyAsync(e->d_dD[k].p, src[k], sizeof(double) * N2,
+                                 r.device_pointers ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+        HFG_CUDA(cudaMemsetAsync(e->d_acc[k].p, 0, sizeof(double) * N2, s));
+        if (mixed)
+        {
+            to_float_kernel<<<grid_for(N2, 256, e->num_sms), 256, 0, s>>>(e->d_dD[k].p, e->d_dDf[k].p, N2);
+            HFG_CUDA(cudaGetLastError());
+        }
+    }
+    HFG_CUDA(cudaEventRecord(e->ev[1], s));
+
+    // Shell-pair maxima.
+    for (int k = 0; k < nspin; ++k)
+    {
+        shell_max_kernel<<<grid_for(e->pairs.size(), 128, e->num_sms), 128, 0, s>>>(
+            e->d_dD[k].p, e->d_pairs.p, static_cast<int>(e->pairs.size()), e->d_mat_off.p, e->d_mat_ld.p, e->d_smax_off.p,
+            e->d_nsh.p, e->d_shnao.p, e->d_smax[k].p);
+        HFG_CUDA(cudaGetLastError());
+    }
+
+    // Lists.
+    const int ncnt = kNumQuartetClasses * 2;
+    e->d_counts.alloc(2 * ncnt + 1);
+    HFG_CUDA(cudaMemsetAsync(e->d_counts.p, 0, sizeof(unsigned long long) * (2 * ncnt + 1), s));
+    int launches = nspin * (mixed ? 2 : 1) + nspin;
+    for (int P1 = 0; P1 < kNumPairClasses; ++P1)
+        for (int P2 = 0; P2 <= P1; ++P2)
+        {
+            const int qc = quartet_class(P1, P2);
+            if (e->cap[qc] == 0 || e->cls_ids[P1].empty() || e->cls_ids[P2].empty())
+                continue;
+            BuildArgs a {};
+            a.ids1 = e->d_cls_ids[P1].p;
+            a.Q1   = e->d_cls_Q[P1].p;
+            a.n1   = static_cast<int>(e->cls_ids[P1].size());
+            a.ids2 = e->d_cls_ids[P2].p;
+            a.Q2   = e->d_cls_Q[P2].p;
+            a.rng2 = e->d_cls_rng[P2].p;
+            a.same_class = P1 == P2;
+            a.pairs = e->d_pairs.p;
+            a.Mt = e->d_smax[0].p;
+            a.Ma = e->d_smax[1].p;
+            a.Mb = uhf ? e->d_smax[2].p : nullptr;
+            a.smax_off = e->d_smax_off.p;
+            a.nsh = e->d_nsh.p;
+            a.sthr = r.schwartz_threshold;
+            a.dthr = r.density_threshold;
+            a.cutoff = r.fp32_cutoff;
+            a.mixed = mixed ? 1 : 0;
+            a.out64 = e->d_list[qc][0].p;
+            a.out32 = mixed ? e->d_list[qc][1].p : nullptr;
+            a.cap = e->cap[qc];
+            a.cnt64 = e->d_counts.p + 2 * qc;
+            a.cnt32 = e->d_counts.p + 2 * qc + 1;
+            a.prim64 = e->d_counts.p + ncnt + 2 * qc;
+            a.prim32 = e->d_counts.p + ncnt + 2 * qc + 1;
+            a.overflow = e->d_counts.p + 2 * ncnt;
+            const long long threads = static_cast<long long>(a.n1) * 32;
+            build_lists_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, s>>>(a);
+            HFG_CUDA(cudaGetLastError());
+            ++launches;
+        }
+    e->h_counts.assign(2 * ncnt + 1, 0);
+    HFG_CUDA(cudaMemcpyAsync(e->h_counts.data(), e->d_counts.p, sizeof(unsigned long long) * (2 * ncnt + 1),
+                             cudaMemcpyDeviceToHost, s));
+    HFG_CUDA(cudaEventRecord(e->ev[2], s));
+    HFG_CUDA(cudaStreamSynchronize(s));
+    if (e->h_counts[2 * ncnt] != 0)
+        throw HfgError(HFG_ERR_OVERFLOW, "fock: quartet list overflow");
+
+    // Class kernels: FP64 lists, then FP32 lists.
+    for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
+    {
+        HFG_CUDA(cudaEventRecord(e->ev[3 + prec], s));
+        for (int qc = kNumQuartetClasses - 1; qc >= 0; --qc)
+        {
+            const unsigned long long n = e->h_counts[2 * qc + prec];
+            if (n == 0)
+                continue;
+            const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+            const int P2 = qc - P1 * (P1 + 1) / 2;
+            const int L  = pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2);
+            ClassLaunch c {};
+            c.list       = e->d_list[qc][prec].p;
+            c.count_dev  = e->d_counts.p + 2 * qc + prec;
+            c.count_host = n;
+            c.view       = base_view(e, prec == 1);
+            c.view.Dt    = prec == 1 ? static_cast<const void*>(e->d_dDf[0].p) : e->d_dD[0].p;
+            c.view.Da    = prec == 1 ? static_cast<const void*>(e->d_dDf[1].p) : e->d_dD[1].p;
+            c.view.Db    = prec == 1 ? static_cast<const void*>(e->d_dDf[2].p) : e->d_dD[2].p;
+            c.view.X     = e->d_acc[0].p;
+            c.view.Ya    = e->d_acc[1].p;
+            c.view.Yb    = e->d_acc[2].p;
+            c.view.ao_thr = r.schwartz_threshold;
+            c.boys_slice = prec == 1 ? static_cast<const void*>(e->d_boys32[L].p) : e->d_boys64[L].p;
+            c.tables     = e->d_tables.p;
+            c.fp32       = prec == 1;
+            c.uhf        = uhf;
+            c.stream     = s;
+            c.num_sms    = e->num_sms;
+            HFG_CUDA(launch_class(qc, c));
+            ++launches;
+        }
+    }
+    HFG_CUDA(cudaEventRecord(e->ev[5], s));
+    double* outs[3] = {r.J, r.K_alpha, r.K_beta};
+    for (int k = 0; k < nspin; ++k)
+    {
+        symmetrize_kernel<<<grid_for(N2, 256, e->num_sms), 256, 0, s>>>(e->d_acc[k].p, e->d_out[k].p, e->d_mat_off.p,
+                                                                          e->d_mat_ld.p, e->nmol, N2);
+        HFG_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    HFG_CUDA(cudaEventRecord(e->ev[6], s));
+    for (int k = 0; k < nspin; ++k)
+        HFG_CUDA(cudaMemcpyAsync(outs[k], e->d_out[k].p, sizeof(double) * N2,
+                                 r.device_pointers ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    HFG_CUDA(cudaStreamSynchronize(s));
+    e->last_valid = true;
+    e->last_mixed = mixed ? 1 : 0;
+    if (st)
+    {
+        std::memset(st, 0, sizeof(*st));
+        for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+        {
+            st->quartets_fp64[qc]      = e->h_counts[2 * qc];
+            st->quartets_fp32[qc]      = e->h_counts[2 * qc + 1];
+            st->prim_quartets_fp64[qc] = e->h_counts[ncnt + 2 * qc];
+            st->prim_quartets_fp32[qc] = e->h_counts[ncnt + 2 * qc + 1];
+            st->flops_fp64 += flops_per_prim_quartet(qc) * st->prim_quartets_fp64[qc] +
+                              flops_per_quartet_digest(qc, uhf) * st->quartets_fp64[qc];
+            st->flops_fp32 += flops_per_prim_quartet(qc) * st->prim_quartets_fp32[qc] +
+                              flops_per_quartet_digest(qc, uhf) * st->quartets_fp32[qc];
+        }
+        float ms = 0.f;
+        HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[1], e->ev[6]));
+        st->ms_total = ms;
+        HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]));
+        st->ms_lists = ms;
+        HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[3], mixed ? e->ev[4] : e->ev[5]));
+        st->ms_eri_fp64 = ms;
+        if (mixed)
+        {
+            HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[4], e->ev[5]));
+            st->ms_eri_fp32 = ms;
+        }
+        st->kernel_launches = launches;
+    }
+}
+
+// Work model (per primitive quartet of class (la lb|lc ld), L = sum): the R recursion (one FMA per
+// R^n_tuv), the ket and bra Hermite->Cartesian transforms with dense Hermite blocks, scaling and Boys;
+// per shell quartet the digestion FMAs (RHF: 2 J + 4 K per integral; UHF adds 4 K_beta).
+double flops_per_prim_quartet(int qc)
+{
+    const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+    const int P2 = qc - P1 * (P1 + 1) / 2;
+    const int la = pair_class_l1(P1), lb = pair_class_l2(P1), lc = pair_class_l1(P2), ld = pair_class_l2(P2);
+    const int L = la + lb + lc + ld;
+    const double nab = ncart(la) * ncart(lb), ncd = ncart(lc) * ncart(ld);
+    const double hab = nherm(la + lb), hcd = nherm(lc + ld);
+    const double cL4 = (L + 1.0) * (L + 2.0) * (L + 3.0) * (L + 4.0) / 24.0;
+    return 2.0 * cL4 + 2.0 * hab * ncd * hcd + 2.0 * nab * ncd * hab + 2.0 * nab * ncd + (2.0 * (L + 1) + 10.0);
+}
+
+double flops_per_quartet_digest(int qc, bool uhf)
+{
+    const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+    const int P2 = qc - P1 * (P1 + 1) / 2;
+    const double n = ncart(pair_class_l1(P1)) * ncart(pair_class_l2(P1)) * ncart(pair_class_l1(P2)) * ncart(pair_class_l2(P2));
+    return (uhf ? 20.0 : 12.0) * n;
+}
+} // namespace hfg
+
+// ------------------------------------------------------------------------------------------------
+// C ABI.
+// ------------------------------------------------------------------------------------------------
+using hfg::HfgError;
+
+template <typename F> static int guarded(hfg_engine* e, F&& f)
+{
+    try
+    {
+        f();
+        return HFG_OK;
+    }
+    catch (const HfgError& x)
+    {
+        if (e)
+            e->last_error = x.what();
+        else
+            hfg::g_create_error = x.what();
+        return x.code;
+    }
+    catch (const std::bad_alloc&)
+    {
+        if (e)
+            e->last_error = "host allocation failed";
+        return HFG_ERR_NOMEM;
+    }
+    catch (const std::exception& x)
+    {
+        if (e)
+            e->last_error = x.what();
+        else
+            hfg::g_create_error = x.what();
+        return HFG_ERR_INVALID;
+    }
+}
+
+extern "C" {
+
+const char* hfg_version(void) { return "hfgpu 0.1 (sm_103a)"; }
+
+int hfg_create_batch(const hfg_basis* bases, int nmol, int device, hfg_engine** out)
+{
+    if (!out || !bases || nmol <= 0)
+    {
+        hfg::g_create_error = "hfg_create: null argument or empty batch";
+        return HFG_ERR_INVALID;
+    }
+    *out = nullptr;
+    auto e = std::make_unique<hfg_engine>();
+    const int rc = guarded(nullptr, [&] {
+        int ndev = 0;
+        HFG_CUDA(cudaGetDeviceCount(&ndev));
+        if (device < 0 || device >= ndev)
+            throw HfgError(HFG_ERR_INVALID, "hfg_create: device index out of range");
+        e->device = device;
+        HFG_CUDA(cudaSetDevice(device));
+        HFG_CUDA(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device));
+        HFG_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        for (auto& ev : e->ev) HFG_CUDA(cudaEventCreate(&ev));
+        e->nmol = nmol;
+        e->basis.resize(nmol);
+        long long mat = 0, smax = 0;
+        int sh = 0;
+        for (int m = 0; m < nmol; ++m)
+        {
+            hfg::validate_and_copy(bases[m], e->basis[m]);
+            hfg::MolInfo mi {};
+            mi.nshells  = bases[m].nshells;
+            mi.nao      = bases[m].nao;
+            mi.sh_off   = sh;
+            mi.mat_off  = mat;
+            mi.smax_off = smax;
+            e->mols.push_back(mi);
+            mat += static_cast<long long>(mi.nao) * mi.nao;
+            smax += static_cast<long long>(mi.nshells) * mi.nshells;
+            sh += mi.nshells;
+        }
+        e->mat_total     = mat;
+        e->smax_total    = smax;
+        e->nshells_total = sh;
+        hfg::pack_molecules(e.get());
+    });
+    if (rc != HFG_OK)
+    {
+        if (e->stream)
+        {
+            cudaStreamDestroy(e->stream);
+            e->stream = nullptr;
+        }
+        return rc;
+    }
+    *out = e.release();
+    return HFG_OK;
+}
+
+int hfg_create(const hfg_basis* basis, int device, hfg_engine** out) { return hfg_create_batch(basis, 1, device, out); }
+
+void hfg_destroy(hfg_engine* e)
+{
+    if (!e)
+        return;
+    cudaSetDevice(e->device);
+    if (e->stream)
+        cudaStreamSynchronize(e->stream);
+    for (auto& ev : e->ev)
+        if (ev)
+            cudaEventDestroy(ev);
+    if (e->stream)
+        cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+const char* hfg_last_error(const hfg_engine* e) { return e ? e->last_error.c_str() : hfg::g_create_error.c_str(); }
+
+void* hfg_stream(hfg_engine* e) { return e ? static_cast<void*>(e->stream) : nullptr; }
+
+int hfg_schwartz(hfg_engine* e, double* Q)
+{
+    if (!e || !Q)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        if (!e->have_Q)
+        {
+            hfg::compute_schwartz(e);
+            hfg::sort_classes(e);
+        }
+        std::vector<long long> qoff(e->nmol, 0);
+        long long acc = 0;
+        for (int m = 0; m < e->nmol; ++m)
+        {
+            qoff[m] = acc;
+            acc += static_cast<long long>(e->mols[m].nshells) * e->mols[m].nshells;
+        }
+        std::fill(Q, Q + acc, 0.0);
+        for (size_t k = 0; k < e->pairs.size(); ++k)
+        {
+            const auto& p = e->pairs[k];
+            const int ns  = e->mols[p.mol].nshells;
+            Q[qoff[p.mol] + p.sh1 + static_cast<long long>(p.sh2) * ns] = e->Qpair[k];
+            Q[qoff[p.mol] + p.sh2 + static_cast<long long>(p.sh1) * ns] = e->Qpair[k];
+        }
+    });
+}
+
+int hfg_set_schwartz(hfg_engine* e, const double* Q)
+{
+    if (!e || !Q)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        e->Qpair.assign(e->pairs.size(), 0.0);
+        long long acc = 0;
+        std::vector<long long> qoff(e->nmol, 0);
+        for (int m = 0; m < e->nmol; ++m)
+        {
+            qoff[m] = acc;
+            acc += static_cast<long long>(e->mols[m].nshells) * e->mols[m].nshells;
+        }
+        for (size_t k = 0; k < e->pairs.size(); ++k)
+        {
+            const auto& p = e->pairs[k];
+            const int ns  = e->mols[p.mol].nshells;
+            // The reference reads Q(a, b) with a >= b (SCF.cpp:606); take that element.
+            const int a = std::max(p.sh1, p.sh2), b = std::min(p.sh1, p.sh2);
+            const double v = Q[qoff[p.mol] + a + static_cast<long long>(b) * ns];
+            if (!(v >= 0.0) || !std::isfinite(v))
+                throw HfgError(HFG_ERR_INVALID, "hfg_set_schwartz: Q must be finite and >= 0");
+            e->Qpair[k] = v;
+        }
+        hfg::sort_classes(e);
+    });
+}
+
+int hfg_fock_direct(hfg_engine* e, const hfg_fock_request* req, hfg_fock_stats* stats)
+{
+    if (!e || !req)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        hfg::fock_direct(e, *req, stats);
+    });
+}
+
+int hfg_survivors(hfg_engine* e, int* quartets, long long cap, long long* count)
+{
+    if (!e || !count)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        if (!e->last_valid)
+            throw HfgError(HFG_ERR_INVALID, "hfg_survivors: no Fock build yet");
+        HFG_CUDA(cudaSetDevice(e->device));
+        std::vector<std::array<int, 5>> all;
+        for (int qc = 0; qc < hfg::kNumQuartetClasses; ++qc)
+            for (int prec = 0; prec < 2; ++prec)
+            {
+                const unsigned long long n = e->h_counts[2 * qc + prec];
+                if (n == 0)
+                    continue;
+                std::vector<hfg::Quartet> q(n);
+                HFG_CUDA(cudaMemcpy(q.data(), e->d_list[qc][prec].p, sizeof(hfg::Quartet) * n, cudaMemcpyDeviceToHost));
+                for (const auto& x : q)
+                {
+                    const auto& P = e->pairs[x.bra];
+                    const auto& K = e->pairs[x.ket];
+                    int a = std::max(P.sh1, P.sh2), b = std::min(P.sh1, P.sh2);
+                    int c = std::max(K.sh1, K.sh2), d = std::min(K.sh1, K.sh2);
+                    const long long ab = static_cast<long long>(a) * (a + 1) / 2 + b;
+                    const long long cd = static_cast<long long>(c) * (c + 1) / 2 + d;
+                    if (ab < cd)
+                    {
+                        std::swap(a, c);
+                        std::swap(b, d);
+                    }
+                    all.push_back({P.mol, a, b, c, d});
+                }
+            }
+        std::sort(all.begin(), all.end());
+        *count = static_cast<long long>(all.size());
+        if (quartets)
+            for (long long k = 0; k < std::min<long long>(cap, *count); ++k)
+                for (int j = 0; j < 4; ++j) quartets[4 * k + j] = all[k][j + 1];
+    });
+}
+
+int hfg_eri_block(hfg_engine* e, int a, int b, int c, int d, double* out)
+{
+    if (!e || !out || e->nmol != 1)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        const int ns = e->mols[0].nshells;
+        if (a < 0 || b < 0 || c < 0 || d < 0 || a >= ns || b >= ns || c >= ns || d >= ns)
+            throw HfgError(HFG_ERR_INVALID, "hfg_eri_block: shell index out of range");
+        auto pair_id = [&](int x, int y) -> int {
+            const int hi = std::max(x, y), lo = std::min(x, y);
+            // pairs are generated in (s1 desc-major) order: s1 = 0.., s2 = 0..s1
+            return hi * (hi + 1) / 2 + lo;
+        };
+        const int pb = pair_id(a, b), pk = pair_id(c, d);
+        const int cb = e->pair_class_of[pb], ck = e->pair_class_of[pk];
+        int bra = pb, ket = pk;
+        if (cb < ck)
+            std::swap(bra, ket);
+        const int qc = hfg::qclass_of(cb, ck);
+        hfg::eval_store(e, qc, {hfg::Quartet {static_cast<uint32_t>(bra), static_cast<uint32_t>(ket)}});
+        const auto& B = e->pairs[bra];
+        const auto& K = e->pairs[ket];
+        const auto& hb = e->basis[0];
+        const int n1 = hfg::ncart(hb.l[B.sh1]), n2 = hfg::ncart(hb.l[B.sh2]), n3 = hfg::ncart(hb.l[K.sh1]), n4 = hfg::ncart(hb.l[K.sh2]);
+        std::vector<double> blk(static_cast<size_t>(n1) * n2 * n3 * n4);
+        HFG_CUDA(cudaMemcpyAsync(blk.data(), e->d_store.p, sizeof(double) * blk.size(), cudaMemcpyDeviceToHost, e->stream));
+        HFG_CUDA(cudaStreamSynchronize(e->stream));
+        // blk is [B.sh1][B.sh2][K.sh1][K.sh2]; permute into [a][b][c][d].
+        const int na = hfg::ncart(hb.l[a]), nb = hfg::ncart(hb.l[b]), nc = hfg::ncart(hb.l[c]), nd = hfg::ncart(hb.l[d]);
+        for (int i = 0; i < na; ++i)
+            for (int j = 0; j < nb; ++j)
+                for (int k = 0; k < nc; ++k)
+                    for (int l = 0; l < nd; ++l)
+                    {
+                        // Map (shell, component) pairs of the request to the stored orientation.
+                        int comp[4];
+                        const int sh[4] = {a, b, c, d}, cc[4] = {i, j, k, l};
+                        const bool swap_pairs = (bra != pb);
+                        const int p0 = swap_pairs ? 2 : 0, p1 = swap_pairs ? 0 : 2;
+                        // bra pair holds request slots p0, p0+1
+                        auto place = [&](int slot_a, int slot_b, const hfg::PairRec& pr, int* dst) {
+                            if (sh[slot_a] == pr.sh1 && (sh[slot_b] == pr.sh2))
+                            {
+                                dst[0] = cc[slot_a];
+                                dst[1] = cc[slot_b];
+                            }
+                            else
+                            {
+                                dst[0] = cc[slot_b];
+                                dst[1] = cc[slot_a];
+                            }
+                        };
+                        place(p0, p0 + 1, B, comp);
+                        place(p1, p1 + 1, K, comp + 2);
+                        out[((i * nb + j) * nc + k) * nd + l] = blk[((comp[0] * n2 + comp[1]) * n3 + comp[2]) * n4 + comp[3]];
+                    }
+        e->d_store.release();
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,40 @@
+// Internal engine state and the per-class launcher interface.
+#pragma once
+
+#include "hfg_common.cuh"
+#include "eri_warp.cuh"
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+namespace hfg
+{
+// Launches the class kernel of one quartet class for one list.
+struct ClassLaunch
+{
+    const Quartet* list;
+    const unsigned long long* count_dev;
+    unsigned long long count_host;
+    FockView view;
+    const void* boys_slice; // slice of the class's total L, Real of the precision
+    const WarpTables* tables;
+    bool fp32;
+    bool uhf;
+    cudaStream_t stream;
+    int num_sms;
+};
+using ClassLauncher = cudaError_t (*)(const ClassLaunch&);
+// Defined in classes.cu (one translation unit per quartet class).
+cudaError_t launch_class(int qclass, const ClassLaunch& L);
+bool class_uses_warp_kernel(int qclass);
+
+// Schwartz kernel launch for pair class pc (defined in classes_schwartz.cu).
+cudaError_t launch_schwartz(int pc, const int* pair_ids, int npairs, const FockView& v, const double* boys_slice,
+                            double* Q, cudaStream_t stream, int num_sms);
+
+// Work model: algorithmic FLOPs of one primitive quartet and of one shell quartet's digestion.
+double flops_per_prim_quartet(int qclass);
+double flops_per_quartet_digest(int qclass, bool uhf);
+} // namespace hfg

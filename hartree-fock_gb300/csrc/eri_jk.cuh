@@ -1,0 +1,426 @@
+// Fused McMurchie-Davidson ERI evaluation + J/K digestion for one shell-quartet class.
+//
+// Reference counterpart: IntegralEngine::electronRepulsion (src/IntegralEngine.cpp:731-992) fused with
+// the digestion loop of SCF::buildFockMatrixDirect (src/SCF.cpp:630-711).
+//
+// One thread evaluates one surviving shell quartet (ab|cd) of class (LA LB | LC LD), LA >= LB,
+// LC >= LD, with every loop over Cartesian components, Hermite indices and expansion coefficients
+// unrolled at compile time (static_for), so the R, G and ERI arrays are register arrays.  The
+// contraction order per quartet:
+//
+//   for each bra primitive pair:   G[tuv][kl] = sum_{ket prims} sum_{tau nu phi} (-1)^{tau+nu+phi}
+//                                               E^{kl}_{tau nu phi} R_{t+tau, u+nu, v+phi}
+//                                  ERI[ij][kl] += sum_{tuv} E^{ij}_{tuv} G[tuv][kl]
+//
+// with R^n_{000} = pref * (-2 rho)^n F_n (the Boys values carry the whole primitive prefactor
+// 2 pi^{5/2} / (p q sqrt(p+q)) * K_ab K_cd * coefficients * radial norms).  The 3-D Hermite tables
+// E^{ij}_{tuv} of each primitive pair are precomputed once per engine (they depend only on the pair),
+// which removes the per-quartet E recursion of the reference (IntegralEngine.cpp:805-820).
+//
+// Digestion: with s = (a==b ? 1/2 : 1)(c==d ? 1/2 : 1)(ab==cd ? 1/2 : 1) and v = s*(ij|kl),
+//   X[i,j] += 2 v dDt[k,l]    X[k,l] += 2 v dDt[i,j]
+//   Y[i,k] += v dDs[j,l]      Y[i,l] += v dDs[j,k]    Y[j,k] += v dDs[i,l]    Y[j,l] += v dDs[i,k]
+// and afterwards J = X + X^T, K = Y + Y^T.  This covers every permutation of every unique integral once,
+// which is what the reference's AO-level symmetry factors (SCF.cpp:665-707) achieve; the reference's
+// AO-level skip |(ij|kl)| < SCHWARTZ_THRESH (SCF.cpp:669-671) is applied to the same contracted values.
+// Per-quartet partial sums are formed in registers and added to X/Y once per quartet.
+#pragma once
+
+#include "boys.cuh"
+#include "hfg_common.cuh"
+
+namespace hfg
+{
+constexpr double kTwoPi25 = 34.98683665524972497; // 2 pi^{5/2}
+
+// Device view of everything a class kernel needs.
+struct FockView
+{
+    const PairRec* pairs;
+    const void* pptab[kNumPairClasses]; // per pair class: primitive-pair records (Real of the kernel)
+    const void* Dt;                     // dD_tot   (double for FP64 kernels, float for FP32 kernels)
+    const void* Da;                     // dD_alpha
+    const void* Db;                     // dD_beta (UHF)
+    double* X;                          // J accumulator (J = X + X^T)
+    double* Ya;                         // K_alpha accumulator
+    double* Yb;                         // K_beta accumulator (UHF)
+    const long long* mat_off;           // per molecule: offset of its n x n block in the packed matrices
+    const int* mat_ld;                  // per molecule: n
+    double ao_thr;                      // AO-level skip threshold (SCHWARTZ_THRESH)
+    double* store;                      // if set: write the quartets' integrals here instead of digesting
+};
+
+__device__ constexpr double ang_norm(int l, int c)
+{
+    const int i = cart_exp(l, c, 0), j = cart_exp(l, c, 1), k = cart_exp(l, c, 2);
+    const int d = dfact_odd(2 * i - 1) * dfact_odd(2 * j - 1) * dfact_odd(2 * k - 1);
+    return d == 1 ? 1.0 : (d == 3 ? 0.57735026918962576451 : (d == 9 ? 1.0 / 3.0 : (d == 15 ? 0.25819888974716112568 : 1.0)));
+}
+
+// Enumerates Hermite triples of total degree <= L by descending degree: k-th entry's hidx(., ., ., L).
+__host__ __device__ constexpr int herm_desc(int k, int L)
+{
+    int n = 0;
+    for (int d = L; d >= 0; --d)
+        for (int v = 0; v <= d; ++v)
+            for (int u = 0; u <= d - v; ++u)
+            {
+                if (n == k)
+                    return hidx(d - u - v, u, v, L);
+                ++n;
+            }
+    return 0;
+}
+
+// R^0_{tuv} for t+u+v <= L into R[hidx(t,u,v,L)], from Fs[n] = pref (-2 rho)^n F_n, in place,
+// level by level (IntegralEngine.cpp:1082-1162 computes the same recursion in a dense 4-D buffer).
+template <int L, typename Real>
+__device__ __forceinline__ void hermite_R(const Real* Fs, Real X, Real Y, Real Z, Real* R)
+{
+    R[0] = Fs[L];
+    static_for<0, L>(
+        [&](auto NN)
+        {
+            constexpr int n = L - 1 - decltype(NN)::value;
+            static_for<0, nherm(L)>(
+                [&](auto KK)
+                {
+                    constexpr int h = herm_desc(decltype(KK)::value, L);
+                    constexpr int t = htuv(h, L, 0), u = htuv(h, L, 1), v = htuv(h, L, 2);
+                    constexpr int d = t + u + v;
+                    if constexpr (d >= 1 && d <= L - n)
+                    {
+                        if constexpr (t > 0)
+                        {
+                            if constexpr (t >= 2)
+                                R[h] = X * R[hidx(t - 1, u, v, L)] + Real(t - 1) * R[hidx(t - 2, u, v, L)];
+                            else
+                                R[h] = X * R[hidx(t - 1, u, v, L)];
+                        }
+                        else if constexpr (u > 0)
+                        {
+                            if constexpr (u >= 2)
+                                R[h] = Y * R[hidx(t, u - 1, v, L)] + Real(u - 1) * R[hidx(t, u - 2, v, L)];
+                            else
+                                R[h] = Y * R[hidx(t, u - 1, v, L)];
+                        }
+                        else
+                        {
+                            if constexpr (v >= 2)
+                                R[h] = Z * R[hidx(t, u, v - 1, L)] + Real(v - 1) * R[hidx(t, u, v - 2, L)];
+                            else
+                                R[h] = Z * R[hidx(t, u, v - 1, L)];
+                        }
+                    }
+                });
+            R[0] = Fs[n];
+        });
+}
+
+// Contracted Cartesian integrals of one quartet (without the angular normalisation factors).
+template <int LA, int LB, int LC, int LD, typename Real>
+__device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& ket, const Real* __restrict__ tb,
+                                             const Real* __restrict__ tk, const Real* __restrict__ slice,
+                                             Real* acc)
+{
+    constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
+    constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
+    constexpr int HAB = nherm(LAB), HL = nherm(L);
+    constexpr int SB = pp_stride(LA, LB), SK = pp_stride(LC, LD);
+#pragma unroll
+    for (int x = 0; x < NAB * NCD; ++x) acc[x] = Real(0);
+
+    for (int ib = 0; ib < bra.npp; ++ib)
+    {
+        const Real* __restrict__ rb = tb + static_cast<size_t>(bra.pp_off + ib) * SB;
+        const Real ip = rb[0], p = rb[1], Px = rb[2], Py = rb[3], Pz = rb[4], Kab = rb[5];
+        Real G[HAB * NCD];
+#pragma unroll
+        for (int x = 0; x < HAB * NCD; ++x) G[x] = Real(0);
+
+        for (int ik = 0; ik < ket.npp; ++ik)
+        {
+            const Real* __restrict__ rk = tk + static_cast<size_t>(ket.pp_off + ik) * SK;
+            const Real iq = rk[0], q = rk[1];
+            const Real X = Px - rk[2], Y = Py - rk[3], Z = Pz - rk[4];
+            const Real rs   = hfg_rsqrt(p + q);
+            const Real rho  = p * q * (rs * rs);
+            const Real pref = Real(kTwoPi25) * (Kab * rk[5]) * (ip * iq) * rs;
+            const Real T    = rho * (X * X + Y * Y + Z * Z);
+            Real F[L + 1];
+            boys_eval<L, Real>(T, slice, F);
+            Real Fs[L + 1];
+            {
+                const Real m2r = Real(-2) * rho;
+                Real w         = pref;
+#pragma unroll
+                for (int n = 0; n <= L; ++n)
+                {
+                    Fs[n] = w * F[n];
+                    w *= m2r;
+                }
+            }
+            Real R[HL];
+            hermite_R<L, Real>(Fs, X, Y, Z, R);
+
+            static_for<0, NCD>(
+                [&](auto KL)
+                {
+                    constexpr int kl   = decltype(KL)::value;
+                    constexpr int lx   = e3_len(LC, LD, kl, 0), ly = e3_len(LC, LD, kl, 1), lz = e3_len(LC, LD, kl, 2);
+                    constexpr int eoff = kPairHeader + e3_offset(LC, LD, kl);
+                    static_for<0, HAB>(
+                        [&](auto TUV)
+                        {
+                            constexpr int h = decltype(TUV)::value;
+                            constexpr int t = htuv(h, LAB, 0), u = htuv(h, LAB, 1), v = htuv(h, LAB, 2);
+                            Real s          = Real(0);
+                            static_for<0, lx * ly * lz>(
+                                [&](auto EE)
+                                {
+                                    constexpr int e   = decltype(EE)::value;
+                                    constexpr int tau = e % lx, nu = (e / lx) % ly, phi = e / (lx * ly);
+                                    const Real term   = rk[eoff + e] * R[hidx(t + tau, u + nu, v + phi, L)];
+                                    if constexpr (((tau + nu + phi) & 1) != 0)
+                                        s -= term;
+                                    else
+                                        s += term;
+                                });
+                            G[h * NCD + kl] += s;
+                        });
+                });
+        }
+
+        static_for<0, NAB>(
+            [&](auto IJ)
+            {
+                constexpr int ij   = decltype(IJ)::value;
+                constexpr int lx   = e3_len(LA, LB, ij, 0), ly = e3_len(LA, LB, ij, 1), lz = e3_len(LA, LB, ij, 2);
+                constexpr int eoff = kPairHeader + e3_offset(LA, LB, ij);
+#pragma unroll
+                for (int kl = 0; kl < NCD; ++kl)
+                {
+                    Real s = Real(0);
+                    static_for<0, lx * ly * lz>(
+                        [&](auto EE)
+                        {
+                            constexpr int e = decltype(EE)::value;
+                            constexpr int t = e % lx, u = (e / lx) % ly, v = e / (lx * ly);
+                            s += rb[eoff + e] * G[hidx(t, u, v, LAB) * NCD + kl];
+                        });
+                    acc[ij * NCD + kl] += s;
+                }
+            });
+    }
+}
+
+template <typename Real> __device__ __forceinline__ Real ldD(const void* p, long long i)
+{
+    return static_cast<const Real*>(p)[i];
+}
+
+// Digestion of one evaluated quartet into X, Ya (, Yb).
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF>
+__device__ __forceinline__ void digest_quartet(const PairRec& bra, const PairRec& ket, bool same_pair, const Real* acc,
+                                               const FockView& v)
+{
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    constexpr int NAB = NA * NB, NCD = NC * ND;
+    const long long off = v.mat_off[bra.mol];
+    const int n         = v.mat_ld[bra.mol];
+    const Real s = Real((bra.same ? 0.5 : 1.0) * (ket.same ? 0.5 : 1.0) * (same_pair ? 0.5 : 1.0));
+    const Real thr = Real(v.ao_thr);
+    const int a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
+    auto at = [&](int r, int c) -> long long { return off + r + static_cast<long long>(c) * n; };
+
+    Real Dcd[NCD], Dab[NAB];
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+        for (int l = 0; l < ND; ++l) Dcd[k * ND + l] = ldD<Real>(v.Dt, at(c0 + k, d0 + l));
+#pragma unroll
+    for (int i = 0; i < NA; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j) Dab[i * NB + j] = ldD<Real>(v.Dt, at(a0 + i, b0 + j));
+
+    Real Jab[NAB], Jcd[NCD];
+#pragma unroll
+    for (int x = 0; x < NAB; ++x) Jab[x] = Real(0);
+#pragma unroll
+    for (int x = 0; x < NCD; ++x) Jcd[x] = Real(0);
+
+    constexpr int nspin = UHF ? 2 : 1;
+#pragma unroll
+    for (int spin = 0; spin < nspin; ++spin)
+    {
+        const void* Ds = spin == 0 ? v.Da : v.Db;
+        Real Dbd[NB * ND], Dbc[NB * NC], Dad[NA * ND], Dac[NA * NC];
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+        {
+#pragma unroll
+            for (int l = 0; l < ND; ++l) Dbd[j * ND + l] = ldD<Real>(Ds, at(b0 + j, d0 + l));
+#pragma unroll
+            for (int k = 0; k < NC; ++k) Dbc[j * NC + k] = ldD<Real>(Ds, at(b0 + j, c0 + k));
+        }
+#pragma unroll
+        for (int i = 0; i < NA; ++i)
+        {
+#pragma unroll
+            for (int l = 0; l < ND; ++l) Dad[i * ND + l] = ldD<Real>(Ds, at(a0 + i, d0 + l));
+#pragma unroll
+            for (int k = 0; k < NC; ++k) Dac[i * NC + k] = ldD<Real>(Ds, at(a0 + i, c0 + k));
+        }
+        Real Kac[NA * NC], Kad[NA * ND], Kbc[NB * NC], Kbd[NB * ND];
+#pragma unroll
+        for (int x = 0; x < NA * NC; ++x) Kac[x] = Real(0);
+#pragma unroll
+        for (int x = 0; x < NA * ND; ++x) Kad[x] = Real(0);
+#pragma unroll
+        for (int x = 0; x < NB * NC; ++x) Kbc[x] = Real(0);
+#pragma unroll
+        for (int x = 0; x < NB * ND; ++x) Kbd[x] = Real(0);
+
+        static_for<0, NA>(
+            [&](auto I)
+            {
+                constexpr int i = decltype(I)::value;
+                static_for<0, NB>(
+                    [&](auto Jx)
+                    {
+                        constexpr int j = decltype(Jx)::value;
+                        static_for<0, NC>(
+                            [&](auto Kx)
+                            {
+                                constexpr int k = decltype(Kx)::value;
+                                static_for<0, ND>(
+                                    [&](auto Lx)
+                                    {
+                                        constexpr int l = decltype(Lx)::value;
+                                        constexpr Real an = Real(ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k)
+                                                                 * ang_norm(LD, l));
+                                        const Real eri = acc[(i * NB + j) * NCD + k * ND + l] * an;
+                                        const Real w   = (fabs(eri) < thr) ? Real(0) : s * eri;
+                                        if (spin == 0)
+                                        {
+                                            Jab[i * NB + j] += w * Dcd[k * ND + l];
+                                            Jcd[k * ND + l] += w * Dab[i * NB + j];
+                                        }
+                                        Kac[i * NC + k] += w * Dbd[j * ND + l];
+                                        Kad[i * ND + l] += w * Dbc[j * NC + k];
+                                        Kbc[j * NC + k] += w * Dad[i * ND + l];
+                                        Kbd[j * ND + l] += w * Dac[i * NC + k];
+                                    });
+                            });
+                    });
+            });
+        double* Y = spin == 0 ? v.Ya : v.Yb;
+#pragma unroll
+        for (int i = 0; i < NA; ++i)
+        {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) atomicAdd(Y + at(a0 + i, c0 + k), double(Kac[i * NC + k]));
+#pragma unroll
+            for (int l = 0; l < ND; ++l) atomicAdd(Y + at(a0 + i, d0 + l), double(Kad[i * ND + l]));
+        }
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+        {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) atomicAdd(Y + at(b0 + j, c0 + k), double(Kbc[j * NC + k]));
+#pragma unroll
+            for (int l = 0; l < ND; ++l) atomicAdd(Y + at(b0 + j, d0 + l), double(Kbd[j * ND + l]));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NA; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j) atomicAdd(v.X + at(a0 + i, b0 + j), 2.0 * double(Jab[i * NB + j]));
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+        for (int l = 0; l < ND; ++l) atomicAdd(v.X + at(c0 + k, d0 + l), 2.0 * double(Jcd[k * ND + l]));
+}
+
+// Stage this class's Boys slice in shared memory.
+template <typename Real> __device__ __forceinline__ void stage_boys(const Real* __restrict__ g, Real* s)
+{
+    constexpr int n = BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = g[i];
+    __syncthreads();
+}
+
+// One launch processes the whole surviving list of one class; the list length is read on the device
+// (written by the list builder), so a build needs no host round trip between kernels.
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF>
+__global__ void __launch_bounds__(128) jk_class_kernel(const Quartet* __restrict__ list,
+                                                       const unsigned long long* __restrict__ count, FockView v,
+                                                       const Real* __restrict__ boys_slice)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real* slice                = reinterpret_cast<Real*>(smem_raw);
+    const unsigned long long n = *count;
+    if (static_cast<unsigned long long>(blockIdx.x) * blockDim.x >= n)
+        return;
+    stage_boys<Real>(boys_slice, slice);
+    constexpr int N = ncart(LA) * ncart(LB) * ncart(LC) * ncart(LD);
+    const Real* tb  = static_cast<const Real*>(v.pptab[pair_class(LA, LB)]);
+    const Real* tk  = static_cast<const Real*>(v.pptab[pair_class(LC, LD)]);
+    for (unsigned long long q = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+         q += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+    {
+        const Quartet qt  = list[q];
+        const PairRec bra = v.pairs[qt.bra];
+        const PairRec ket = v.pairs[qt.ket];
+        Real acc[N];
+        eval_quartet<LA, LB, LC, LD, Real>(bra, ket, tb, tk, slice, acc);
+        if (v.store != nullptr)
+        {
+            static_for<0, N>(
+                [&](auto E)
+                {
+                    constexpr int e  = decltype(E)::value;
+                    constexpr int NB = ncart(LB), NC = ncart(LC), ND = ncart(LD), NCD = NC * ND;
+                    constexpr double an = ang_norm(LA, e / NCD / NB) * ang_norm(LB, (e / NCD) % NB)
+                                        * ang_norm(LC, (e % NCD) / ND) * ang_norm(LD, e % ND);
+                    v.store[q * N + e] = double(acc[e]) * an;
+                });
+            continue;
+        }
+        digest_quartet<LA, LB, LC, LD, Real, UHF>(bra, ket, qt.bra == qt.ket, acc, v);
+    }
+}
+
+// Schwartz bound of every pair of one pair class: Q = sqrt(max_ij (ij|ij)) (IntegralEngine.cpp:695-728).
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) schwartz_kernel(const int* __restrict__ pair_ids, int npairs, FockView v,
+                                                       const double* __restrict__ boys_slice, double* __restrict__ Q)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* slice = reinterpret_cast<double*>(smem_raw);
+    stage_boys<double>(boys_slice, slice);
+    constexpr int NAB = ncart(LA) * ncart(LB);
+    const double* tb  = static_cast<const double*>(v.pptab[pair_class(LA, LB)]);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x)
+    {
+        const int pid     = pair_ids[k];
+        const PairRec pr  = v.pairs[pid];
+        double acc[NAB * NAB];
+        eval_quartet<LA, LB, LA, LB, double>(pr, pr, tb, tb, slice, acc);
+        double mx = 0.0;
+        static_for<0, ncart(LA)>(
+            [&](auto I)
+            {
+                static_for<0, ncart(LB)>(
+                    [&](auto Jx)
+                    {
+                        constexpr int i = decltype(I)::value, j = decltype(Jx)::value;
+                        constexpr double an = ang_norm(LA, i) * ang_norm(LB, j);
+                        const double val    = acc[(i * ncart(LB) + j) * NAB + i * ncart(LB) + j] * (an * an);
+                        mx                  = fmax(mx, val);
+                    });
+            });
+        Q[pid] = sqrt(mx);
+    }
+}
+} // namespace hfg

@@ -1,0 +1,139 @@
+/*
+ * hfgpu -- GB300 direct-SCF two-electron (Fock-build) engine: C ABI.
+ *
+ * This is the drop-in boundary for the two-electron path of the reference Hartree-Fock program
+ * (MalachiF1/Hartree-Fock).  The reference has no plugin API; its boundary is the C++ class API of
+ * IntegralEngine and the private SCF::buildFockMatrixDirect.  Each entry point below names the
+ * reference interface it replaces.  Plain pointers and sizes only; matrices are column-major
+ * n x n FP64, exactly Eigen::MatrixXd's layout in the reference.
+ *
+ * Conventions: every function returns HFG_OK (0) or a negative HFG_ERR_* code and never aborts;
+ * hfg_last_error() describes the last failure.  Calls on one engine are not thread-safe; the engine
+ * keeps no caller pointer after a call returns.  Host-pointer calls synchronise before returning.
+ */
+#ifndef HFGPU_H
+#define HFGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HFG_OK 0
+#define HFG_ERR_INVALID -1     /* bad argument (null pointer, size, threshold) */
+#define HFG_ERR_CUDA -2        /* CUDA runtime failure (message in hfg_last_error) */
+#define HFG_ERR_BASIS -3       /* basis data inconsistent (offsets, normalisation factors) */
+#define HFG_ERR_UNSUPPORTED -4 /* angular momentum above d, or a feature not built */
+#define HFG_ERR_NOMEM -5       /* device or host allocation failed */
+#define HFG_ERR_OVERFLOW -6    /* a quartet list exceeded its capacity (internal) */
+
+#define HFG_PRECISION_FP64 0  /* every surviving quartet in FP64 */
+#define HFG_PRECISION_MIXED 1 /* quartets with bound below fp32_cutoff in FP32, the rest in FP64 */
+
+/* The basis as the reference's IntegralEngine holds it (src/IntegralEngine.cpp:13-75,
+ * include/IntegralEngine.hpp:145-168): per shell l, primitive count and offsets, AO offset, offset of
+ * its normalisation factors and centre (bohr); per primitive exponent and contraction coefficient;
+ * per primitive x AO the normalisation factor (src/Basis.cpp:61-77); per AO the Cartesian exponents.
+ * Cartesian order within a shell: x exponent descending, then y descending (src/Basis.cpp:48-59). */
+typedef struct hfg_basis
+{
+    int nshells;
+    int nao;
+    int nprim;             /* total primitives */
+    const int* l;          /* [nshells] */
+    const int* nprim_sh;   /* [nshells] */
+    const int* prim_off;   /* [nshells] */
+    const int* ao_off;     /* [nshells] */
+    const int* norm_off;   /* [nshells] */
+    const double* centers; /* [nshells][3] */
+    const double* alpha;   /* [nprim] */
+    const double* coeff;   /* [nprim] */
+    const double* norms;   /* [sum_s nprim_sh[s]*nao(l[s])] */
+    const int* am;         /* [nao][3] */
+} hfg_basis;
+
+typedef struct hfg_engine hfg_engine;
+
+/* One direct Fock build, SCF::buildFockMatrixDirect (src/SCF.cpp:523-744) without the final
+ * F = F_prev + J - K, which the caller forms exactly as SCF.cpp:731-743 does.
+ * Inputs are the density increments dD = D - D_prev.  Outputs are the full symmetric
+ * J[dD_tot], K_alpha[dD_alpha] (and K_beta[dD_beta] when unrestricted).
+ * For a batch engine every matrix is the concatenation of the molecules' n_m x n_m blocks. */
+typedef struct hfg_fock_request
+{
+    int unrestricted;          /* 0: RHF (dD_beta and K_beta ignored), 1: UHF */
+    int precision;             /* HFG_PRECISION_FP64 or HFG_PRECISION_MIXED */
+    int device_pointers;       /* 1: all matrix pointers below are CUDA device pointers */
+    double schwartz_threshold; /* SCHWARTZ_THRESH: shell quartet and AO-level skip (SCF.cpp:606, 670) */
+    double density_threshold;  /* DENSITY_THRESH (SCF.cpp:610-623) */
+    double fp32_cutoff;        /* MIXED: quartets with Q_ab Q_cd max|dD| below this run in FP32 */
+    const double* dD_tot;      /* D_tot - D_tot_prev */
+    const double* dD_alpha;    /* D_alpha - D_alpha_prev */
+    const double* dD_beta;     /* D_beta - D_beta_prev (UHF) */
+    double* J;
+    double* K_alpha;
+    double* K_beta; /* UHF */
+} hfg_fock_request;
+
+#define HFG_NUM_CLASSES 21 /* shell-quartet classes (la lb | lc ld) for s, p, d */
+
+typedef struct hfg_fock_stats
+{
+    unsigned long long quartets_fp64[HFG_NUM_CLASSES]; /* surviving shell quartets per class */
+    unsigned long long quartets_fp32[HFG_NUM_CLASSES];
+    unsigned long long prim_quartets_fp64[HFG_NUM_CLASSES]; /* primitive quartets evaluated */
+    unsigned long long prim_quartets_fp32[HFG_NUM_CLASSES];
+    double flops_fp64;  /* algorithmic FP64 flops of the build (work model of the engine docs) */
+    double flops_fp32;
+    double ms_total;    /* device time of the build, list building to symmetrisation */
+    double ms_lists;    /* device time of screening + list building */
+    double ms_eri_fp64; /* device time of the FP64 class kernels */
+    double ms_eri_fp32; /* device time of the FP32 class kernels */
+    int kernel_launches;
+} hfg_fock_stats;
+
+/* IntegralEngine::IntegralEngine(const BasisSet&) (include/IntegralEngine.hpp:11).  Packs the basis
+ * into device tables (shell pairs, primitive-pair Hermite tables, Boys grids) on `device`. */
+int hfg_create(const hfg_basis* basis, int device, hfg_engine** out);
+
+/* A batch of independent molecules in one engine: their Fock builds run in one launch per class.
+ * No reference counterpart (the reference handles one molecule per process). */
+int hfg_create_batch(const hfg_basis* bases, int nmol, int device, hfg_engine** out);
+
+void hfg_destroy(hfg_engine* engine);
+
+/* Last error message of `engine` (or of the last failed create when engine is NULL). */
+const char* hfg_last_error(const hfg_engine* engine);
+
+/* IntegralEngine::schwartzScreeningMatrix (include/IntegralEngine.hpp:32, src/IntegralEngine.cpp:695-728):
+ * Q(a,b) = sqrt(max (ab|ab)), nshells x nshells column-major (host pointer).  Batch engines write the
+ * molecules' blocks one after another. */
+int hfg_schwartz(hfg_engine* engine, double* Q);
+
+/* Replace the engine's Schwartz matrix (host, same layout as hfg_schwartz), e.g. with the reference's
+ * own Q so that quartet survival can be compared bit for bit. */
+int hfg_set_schwartz(hfg_engine* engine, const double* Q);
+
+/* SCF::buildFockMatrixDirect (include/SCF.hpp:129, src/SCF.cpp:523-744); `stats` may be NULL. */
+int hfg_fock_direct(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_stats* stats);
+
+/* The surviving canonical shell quartets (a >= b, c >= d, ab >= cd; the reference's loop indices,
+ * SCF.cpp:592-623) of the last hfg_fock_direct call, sorted lexicographically, as 4 ints each.
+ * Returns the count in *count; writes at most `cap` quartets (quartets may be NULL to query). */
+int hfg_survivors(hfg_engine* engine, int* quartets, long long cap, long long* count);
+
+/* IntegralEngine::electronRepulsion(a, b, c, d, std::vector<double>&) (include/IntegralEngine.hpp:26-28,
+ * src/IntegralEngine.cpp:731-992): contracted block, row-major [a][b][c][d], full (no zero pattern). */
+int hfg_eri_block(hfg_engine* engine, int a, int b, int c, int d, double* out);
+
+/* The CUDA stream the engine launches on (a cudaStream_t), for callers that time or order work. */
+void* hfg_stream(hfg_engine* engine);
+
+/* Library version string. */
+const char* hfg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HFGPU_H */

@@ -1,0 +1,87 @@
+"""The CPU oracle (oracle/hf_oracle.c) pinned against the reference's own outputs (golden fixtures,
+generated by tests/golden/make_golden.py from the compiled reference)."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_NAMES, load_golden
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_oracle_schwartz_matches_reference(port, name):
+    g = load_golden(name)
+    B = port.Basis(g["soa"])
+    Q = B.schwartz()
+    assert np.max(np.abs(Q - g["Q"])) <= 1e-14 * max(1.0, np.abs(g["Q"]).max())
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_oracle_fock_matches_reference(port, name):
+    g = load_golden(name)
+    B = port.Basis(g["soa"])
+    uhf = bool(g["unrestricted"])
+    Da, Db = g["Da"], g["Db"]
+    J, Ka, Kb, _ = B.fock_direct(g["Q"], Da + Db, Da, Db if uhf else None)
+    assert np.max(np.abs((J - Ka) - g["Fa"])) <= 1e-11
+    if uhf:
+        assert np.max(np.abs((J - Kb) - g["Fb"])) <= 1e-11
+    # Incremental build from the first one (SCF.cpp:731-732).
+    dA, dB = g["Da2"] - Da, g["Db2"] - Db
+    J2, Ka2, Kb2, _ = B.fock_direct(g["Q"], (g["Da2"] + g["Db2"]) - (Da + Db), dA, dB if uhf else None)
+    assert np.max(np.abs(g["Fa"] + J2 - Ka2 - g["Fa2"])) <= 1e-11
+
+
+@pytest.mark.parametrize("name", ["h2o_631g", "w2_631gss", "w2_ccpvdz"])
+def test_oracle_one_electron_matches_reference(port, name):
+    g = load_golden(name)
+    B = port.Basis(g["soa"])
+    S, T, V = B.one_electron(g["Z"], g["xyz"])
+    for a, b in ((S, g["S"]), (T, g["T"]), (V, g["V"])):
+        assert np.max(np.abs(a - b)) <= 1e-12 * max(1.0, np.abs(b).max())
+
+
+def test_oracle_boys_against_series(port):
+    # Boys.cpp:74-89 series, in exact rational-ish arithmetic via math.fsum of the same terms.
+    rng = np.random.default_rng(3)
+    for _ in range(300):
+        m = int(rng.integers(0, 9))
+        T = float(rng.choice([rng.uniform(0, 2), rng.uniform(0, 30), rng.uniform(30, 60)]))
+        F = port.boys(m, T)
+        for k in range(m + 1):
+            terms, t = [], 1.0 / (k + 0.5)
+            for i in range(400):
+                terms.append(t)
+                t *= T / (k + i + 1.5)
+            ref = math.fsum(terms) * math.exp(-T) / 2
+            tol = 5e-13 if T <= 30 else 5e-7  # above 30 the reference uses the asymptotic form
+            assert abs(F[k] - ref) <= tol * ref, (m, T, k, F[k], ref)
+
+
+def test_oracle_survivors_are_the_reference_predicate(port):
+    g = load_golden("w2_631gss")
+    B = port.Basis(g["soa"])
+    D = g["Da"]
+    surv = B.survivors(g["Q"], 2 * D, D)
+    ns = B.nshells
+    # brute force of SCF.cpp:592-623
+    from itertools import product
+    Qm = g["Q"]
+    l = g["soa"]["l"]
+    off = g["soa"]["ao_off"]
+    n = [(x + 1) * (x + 2) // 2 for x in l]
+    M = np.zeros((ns, ns))
+    for a in range(ns):
+        for b in range(ns):
+            M[a, b] = np.abs(D[off[a]:off[a] + n[a], off[b]:off[b] + n[b]]).max()
+    want = []
+    for a, b, c, d in product(range(ns), repeat=4):
+        if b > a or d > c or a * (a + 1) // 2 + b < c * (c + 1) // 2 + d:
+            continue
+        if Qm[a, b] * Qm[c, d] < 1e-10:
+            continue
+        md = max(2 * 2 * M[a, b], 2 * 2 * M[c, d], M[a, c], M[a, d], M[b, c], M[b, d])
+        if md < 1e-10:
+            continue
+        want.append((a, b, c, d))
+    assert sorted(map(tuple, surv.tolist())) == want
