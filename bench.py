@@ -1,0 +1,407 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 direct-SCF Fock build (one JSON line on stdout, rank 0).
+
+Workload (default): (H2O)_64 on a 4x4x4 lattice, 5.5 bohr spacing, seeded rotations and +-0.2 bohr
+jitter (seed 0), RHF/6-31G** with Cartesian d (768 shells, 1600 basis functions); the density is the
+core-Hamiltonian guess, so every step is the first (full, non-incremental) direct Fock build of the SCF,
+SCHWARTZ_THRESH = DENSITY_THRESH = 1e-10.  A step = one hfg_fock_direct call.
+
+* value      Fock builds/s, mixed FP32/FP64 (quartets whose Q_ab Q_cd max|dD| < 1e-6 in FP32), inputs and
+             outputs resident in HBM (device pointers), all ranks' builds / max time over ranks.
+* e2e        the same build through the C ABI with host buffers: dD_tot and dD_alpha copied in, J and
+             K_alpha copied out, every step.
+* fp64_*     the plain all-FP64 GPU build on the same density, and the energy difference of the two
+             builds' two-electron energies.
+* roofline   the dominant kernel group (the FP64 ERI class kernels), achieved algorithmic FP64 FLOP/s
+             (engine work model) over their CUDA-event time, against the FP64 FMA peak this run measures.
+* cpu_baseline / --impl reference   the C restatement of the reference's OpenMP build (oracle/) timed
+             on this host on a seeded sample of bra shell pairs and scaled to the full build by the
+             number of surviving shell quartets.
+
+Multi-GPU (torchrun): every rank builds the same workload on its own GPU (independent replicas, no
+collective on the data path; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "hartree-fock_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Fock builds/s & SCF time, (H2O)_64/6-31G**: mixed vs FP64 GPU, |ΔE|≤1e-6 Eh"
+WORKLOADS = {
+    "h2o64": dict(lattice=(4, 4, 4), basis="6-31G**", name="(H2O)_64 RHF/6-31G** direct Fock build (1600 bf)"),
+    "h2o16": dict(lattice=(4, 2, 2), basis="6-31G**", name="(H2O)_16 RHF/6-31G** direct Fock build (400 bf)"),
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="h2o64")
+    ap.add_argument("--fp32-cutoff", type=float, default=1e-6)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of one baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scf", action="store_true", help="also time full SCFs (mixed and FP64)")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.world, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as td
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            td.init_process_group(backend)
+            self.td = td
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            import torch
+
+            if torch.cuda.is_available():
+                self.td.barrier(device_ids=[self.local])
+            else:
+                self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while active."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(name):
+    from hfgpu import basis, workloads
+
+    w = WORKLOADS[name]
+    Z, xyz = workloads.water_lattice(*w["lattice"], spacing=5.5, seed=0, jitter=0.2)
+    soa = basis.pack(w["basis"], Z, xyz)
+    return Z, xyz, soa
+
+
+def cpu_baseline(soa, Z, xyz, Da, target_s: float, total_quartets: int | None = None, seed: int = 0):
+    """Time the oracle's OpenMP build on a seeded sample of bra shell pairs; scale to the full build."""
+    import numpy as np
+
+    from oracle import port
+
+    port.build()
+    B = port.Basis(soa)
+    cores = port.lib().orc_num_threads()
+    Q = B.schwartz()
+    dt, da = 2.0 * Da, Da
+    if total_quartets is None:
+        total_quartets = int(B.count_survivors(Q, dt, da))
+    ns = B.nshells
+    npairs = ns * (ns + 1) // 2
+    rng = np.random.default_rng(seed)
+
+    def run(frac):
+        mask = (rng.random(npairs) < frac).astype(np.uint8)
+        t0 = time.perf_counter()
+        _, _, _, n = B.fock_direct_sample(Q, dt, da, mask)
+        return time.perf_counter() - t0, int(n), int(mask.sum())
+
+    frac = 2e-4
+    t, n, m = run(frac)
+    while t < 0.5 and frac < 0.5:  # calibrate to a measurable sample
+        frac *= 4
+        t, n, m = run(frac)
+    per_q = t / max(n, 1)
+    frac = min(1.0, frac * target_s / max(t, 1e-3))
+    t, n, m = run(frac)
+    est = t * total_quartets / max(n, 1)
+    return {"builds_per_s": 1.0 / est, "cores": cores, "sample_seconds": t, "sample_quartets": n,
+            "sample_bra_pairs": m, "total_quartets": total_quartets, "est_build_seconds": est,
+            "calibration_s_per_quartet": per_q}
+
+
+def reference_arm(args, dist):
+    """--impl reference: the reference algorithm (C restatement, OpenMP, all host cores) on this host."""
+    if dist.rank != 0:
+        return
+    import numpy as np
+
+    from hfgpu import basis, workloads
+
+    Z, xyz, soa = make_workload(args.workload)
+    # The core guess needs the GPU host path; the reference arm uses a density of the same structure
+    # built on the CPU: the oracle's one-electron integrals and numpy's eigensolver (FP64).
+    from oracle import port
+
+    port.build()
+    B = port.Basis(soa)
+    S, T, V = B.one_electron(Z, xyz)
+    h = T + V
+    w, U = np.linalg.eigh(S)
+    X = (U * np.where(w > 0, 1.0 / np.sqrt(np.maximum(w, 1e-300)), 0.0)) @ U.T
+    e, Cp = np.linalg.eigh(X.T @ h @ X)
+    C = X @ Cp
+    nocc = (sum(Z)) // 2
+    Da = C[:, :nocc] @ C[:, :nocc].T
+    samples = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(soa, Z, xyz, Da, args.cpu_seconds / 2, seed=i)
+        if i >= args.warmup:
+            samples.append(r)
+    value = statistics.median(s["builds_per_s"] for s in samples)
+    r0 = samples[0]
+    sample = (f"seeded random {r0['sample_bra_pairs']} of {len(soa['l']) * (len(soa['l']) + 1) // 2} bra shell pairs "
+              f"({r0['sample_quartets']} of {r0['total_quartets']} surviving quartets, {r0['sample_seconds']:.1f} s), "
+              f"scaled by quartet count")
+    line = {
+        "metric": METRIC, "value": value, "unit": "Fock builds/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded water lattice)",
+        "config": {"workload": WORKLOADS[args.workload]["name"], "precision": "fp64 (reference algorithm)"},
+        "cpu_baseline": {"value": value, "unit": "Fock builds/s", "cores": r0["cores"], "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Fock builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args, dist):
+    import numpy as np
+    import torch
+
+    from hfgpu.engine import FP64, MIXED, Engine, measure_fma_peak
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    Z, xyz, soa = make_workload(args.workload)
+    eng = Engine(soa, device=dev)
+    Da, _ = eng.core_guess(Z, xyz, 0, 1)
+    n = eng.nao
+    t64 = lambda a: torch.from_numpy(np.asfortranarray(a).ravel(order="F")).to(f"cuda:{dev}")
+    d_dt, d_da = t64(2.0 * Da), t64(Da)
+    d_J = torch.zeros(n * n, dtype=torch.float64, device=f"cuda:{dev}")
+    d_K = torch.zeros_like(d_J)
+    ptrs = dict(dD_tot=d_dt.data_ptr(), dD_alpha=d_da.data_ptr(), J=d_J.data_ptr(), K_alpha=d_K.data_ptr())
+    stream = torch.cuda.ExternalStream(eng.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")  # > L2 (129 MB)
+
+    def build(prec):
+        return eng.fock_device(ptrs, precision=prec, fp32_cutoff=args.fp32_cutoff)
+
+    # Warm-up (also computes the Schwartz matrix and sizes the quartet lists).
+    for _ in range(max(args.warmup, 1)):
+        st = build(MIXED)
+    torch.cuda.synchronize()
+
+    # Timed region: K mixed builds, device resident.
+    dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    with ClockSampler(dev) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            stats.append(build(MIXED))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = dist.max(ms)
+    value = dist.world * args.steps / (ms_max / 1000.0)
+    st = stats[-1]
+    J_mixed = d_J.cpu().numpy().reshape(n, n, order="F")
+    K_mixed = d_K.cpu().numpy().reshape(n, n, order="F")
+
+    # End to end through the C ABI with host buffers.
+    Dt_h, Da_h = np.asfortranarray(2.0 * Da), np.asfortranarray(Da)
+    eng.fock(Dt_h, Da_h, precision=MIXED, fp32_cutoff=args.fp32_cutoff)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        Jh, Kh, _, _ = eng.fock(Dt_h, Da_h, precision=MIXED, fp32_cutoff=args.fp32_cutoff)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.world * args.steps / e2e_s
+
+    # Plain FP64 GPU build on the same density.
+    build(FP64)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    k64 = max(1, min(2, args.steps))
+    for _ in range(k64):
+        st64 = build(FP64)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    fp64_value = dist.world * k64 / (dist.max(ev0.elapsed_time(ev1)) / 1000.0)
+    J64 = d_J.cpu().numpy().reshape(n, n, order="F")
+    K64 = d_K.cpu().numpy().reshape(n, n, order="F")
+    # Two-electron energy of the build for the guess density, RHF: E2 = tr(Da (J - K_alpha)).
+    e2_mixed = float(np.sum(Da * (J_mixed - K_mixed)))
+    e2_fp64 = float(np.sum(Da * (J64 - K64)))
+
+    peak64 = measure_fma_peak(True, dev)
+    peak32 = measure_fma_peak(False, dev)
+    ach64 = st["flops_fp64"] / (st["ms_eri_fp64"] * 1e-3) / 1e12 if st["ms_eri_fp64"] > 0 else 0.0
+    ach32 = st["flops_fp32"] / (st["ms_eri_fp32"] * 1e-3) / 1e12 if st["ms_eri_fp32"] > 0 else 0.0
+
+    out = None
+    if dist.rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            nq = sum(st["quartets_fp64"]) + sum(st["quartets_fp32"])
+            r = cpu_baseline(soa, Z, xyz, Da, args.cpu_seconds, total_quartets=nq)
+            cpu = {"value": r["builds_per_s"], "unit": "Fock builds/s", "cores": r["cores"], "kind": "port",
+                   "sample": (f"seeded random {r['sample_bra_pairs']} bra shell pairs, {r['sample_quartets']} of "
+                              f"{r['total_quartets']} surviving quartets in {r['sample_seconds']:.1f} s, scaled by "
+                              f"quartet count")}
+        out = {
+            "metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (seeded water lattice, core-guess density)",
+            "config": {"workload": WORKLOADS[args.workload]["name"], "precision": "mixed FP32/FP64",
+                       "fp32_cutoff": args.fp32_cutoff, "schwartz_thresh": 1e-10, "density_thresh": 1e-10,
+                       "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas x{dist.world}"},
+            "fp64_builds_per_s": fp64_value,
+            "speedup_mixed_vs_fp64": value / fp64_value if fp64_value else None,
+            "delta_e2_mixed_vs_fp64": abs(e2_mixed - e2_fp64),
+            "max_abs_dF_mixed_vs_fp64": float(max(np.abs(J_mixed - J64).max(), np.abs(K_mixed - K64).max())),
+            "quartets": {"fp64": int(sum(st["quartets_fp64"])), "fp32": int(sum(st["quartets_fp32"])),
+                         "prim_fp64": int(sum(st["prim_quartets_fp64"])), "prim_fp32": int(sum(st["prim_quartets_fp32"]))},
+            "device_ms": {"build": st["ms_total"], "lists": st["ms_lists"], "eri_fp64": st["ms_eri_fp64"],
+                          "eri_fp32": st["ms_eri_fp32"], "fp64_build": st64["ms_total"]},
+            "roofline": {"bound": "fp64", "kernel": "FP64 ERI class kernels (jk_class*_kernel<double>)",
+                         "achieved": ach64, "peak": peak64, "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 else None,
+                         "peak_source": "measured FP64 FMA loop (hfg_measure_fma_peak) on this GPU",
+                         "traffic": None,
+                         "fp32_kernels": {"achieved": ach32, "peak": peak32,
+                                          "frac": ach32 / peak32 if peak32 else None}},
+            "e2e": {"value": e2e_value, "unit": "Fock builds/s", "h2d_bytes_per_step": 2 * n * n * 8,
+                    "d2h_bytes_per_step": 2 * n * n * 8},
+            "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        if args.scf:
+            out["scf"] = scf_timings(soa, Z, xyz, dev, args.fp32_cutoff)
+    return out
+
+
+def scf_timings(soa, Z, xyz, dev, cutoff):
+    from hfgpu.engine import FP64, MIXED, Engine
+
+    res = {}
+    for tag, prec in (("fp64", FP64), ("mixed", MIXED)):
+        eng = Engine(soa, device=dev)
+        r, _, _ = eng.scf(Z, xyz, 0, 1, dict(precision=prec, fp32_cutoff=cutoff, energy_tol=1e-8, density_tol=1e-6,
+                                              diis_tol=1e-6, max_iter=60))
+        res[tag] = {"seconds": r["ms_total"] / 1000.0, "fock_seconds": r["ms_fock"] / 1000.0,
+                    "iterations": r["iterations"], "converged": r["converged"], "e_total": r["e_total"]}
+        eng.close()
+    res["delta_e"] = abs(res["mixed"]["e_total"] - res["fp64"]["e_total"])
+    res["speedup"] = res["fp64"]["seconds"] / res["mixed"]["seconds"]
+    return res
+
+
+def main():
+    args = parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            reference_arm(args, dist)
+        else:
+            out = gpu_arm(args, dist)
+            if out is not None:
+                print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -91,8 +91,9 @@ struct MolInfo
 // Host-side basis of one molecule (copied from the caller).
 struct HostBasis
 {
-    std::vector<int> l, nprim, prim_off, ao_off;
-    std::vector<double> centers, alpha, coeff, radial; // radial: coeff-free radial norm per primitive
+    std::vector<int> l, nprim, prim_off, ao_off, norm_off, am;
+    std::vector<double> centers, alpha, coeff, norms, radial; // radial: coeff-free radial norm per primitive
+    hfg_basis view {};
 };
 } // namespace
 } // namespace hfg
@@ -366,6 +367,18 @@ void validate_and_copy(const hfg_basis& b, HostBasis& hb)
     hb.alpha.assign(b.alpha, b.alpha + b.nprim);
     hb.coeff.assign(b.coeff, b.coeff + b.nprim);
     hb.radial.assign(b.nprim, 0.0);
+    hb.norm_off.assign(b.norm_off, b.norm_off + b.nshells);
+    hb.am.assign(b.am, b.am + 3 * b.nao);
+    {
+        size_t nn = 0;
+        for (int s = 0; s < b.nshells; ++s)
+        {
+            if (b.l[s] < 0 || b.l[s] > kMaxL || b.nprim_sh[s] <= 0)
+                break;
+            nn = std::max(nn, static_cast<size_t>(b.norm_off[s]) + static_cast<size_t>(b.nprim_sh[s]) * ncart(b.l[s]));
+        }
+        hb.norms.assign(b.norms, b.norms + nn);
+    }
     int ao = 0;
     for (int s = 0; s < b.nshells; ++s)
     {
@@ -407,6 +420,9 @@ void validate_and_copy(const hfg_basis& b, HostBasis& hb)
     }
     if (ao != b.nao)
         throw HfgError(HFG_ERR_BASIS, "basis: nao does not match the shells");
+    hb.view = hfg_basis {b.nshells, b.nao, b.nprim, hb.l.data(), hb.nprim.data(), hb.prim_off.data(), hb.ao_off.data(),
+                         hb.norm_off.data(), hb.centers.data(), hb.alpha.data(), hb.coeff.data(), hb.norms.data(),
+                         hb.am.data()};
 }
 
 // 1-D Hermite coefficients E^{ij}_t of one axis for i <= l1, j <= l2 (McMurchie-Davidson recurrences;
@@ -876,6 +892,17 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
         }
         st->kernel_launches = launches;
     }
+}
+
+const hfg_basis* engine_basis(const hfg_engine* e)
+{
+    return (e && e->nmol == 1) ? &e->basis[0].view : nullptr;
+}
+
+void engine_set_error(hfg_engine* e, const std::string& msg)
+{
+    if (e)
+        e->last_error = msg;
 }
 
 // Work model (per primitive quartet of class (la lb|lc ld), L = sum): the R recursion (one FMA per

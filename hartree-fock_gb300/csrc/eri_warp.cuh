@@ -16,6 +16,8 @@
 
 #include "eri_jk.cuh"
 
+#include <cuda_runtime.h>
+
 namespace hfg
 {
 // Lookup tables for the runtime loops of the warp kernel, built once by the engine.

@@ -59,7 +59,7 @@ def _units():
         src = os.path.join(CSRC, "classes.cu")
         flags = NVCC_FLAGS + [f"-DHFG_QCLASS={c}"]
         units.append(("nvcc", src, flags, f"class{c:02d}", hdrs))
-    for name in ("engine.cu", "dispatch.cu"):
+    for name in ("engine.cu", "dispatch.cu", "peak.cu"):
         units.append(("nvcc", os.path.join(CSRC, name), NVCC_FLAGS, name[:-3], hdrs))
     for name in sorted(os.listdir(CSRC)):
         if name.endswith(".cpp"):

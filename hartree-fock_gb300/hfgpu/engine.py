@@ -47,6 +47,28 @@ class Stats(ctypes.Structure):
         return d
 
 
+class ScfOptions(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("energy_tol", ctypes.c_double), ("density_tol", ctypes.c_double),
+                ("use_diis", ctypes.c_int), ("diis_size", ctypes.c_int), ("diis_tol", ctypes.c_double),
+                ("unrestricted", ctypes.c_int), ("guess_mix", ctypes.c_int), ("damp", ctypes.c_int),
+                ("max_damp_iter", ctypes.c_int), ("stop_damp_thresh", ctypes.c_double),
+                ("level_shift", ctypes.c_double), ("lshift_gap_tol", ctypes.c_double),
+                ("max_lshift_iter", ctypes.c_double), ("stop_lshift_thresh", ctypes.c_double),
+                ("schwartz_threshold", ctypes.c_double), ("density_threshold", ctypes.c_double),
+                ("precision", ctypes.c_int), ("fp32_cutoff", ctypes.c_double), ("full_rebuild_every", ctypes.c_int),
+                ("verbose", ctypes.c_int)]
+
+
+class ScfResult(ctypes.Structure):
+    _fields_ = [("e_electronic", ctypes.c_double), ("e_nuclear", ctypes.c_double), ("e_total", ctypes.c_double),
+                ("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("delta_e", ctypes.c_double),
+                ("delta_d", ctypes.c_double), ("diis_error", ctypes.c_double), ("ms_total", ctypes.c_double),
+                ("ms_fock", ctypes.c_double), ("fock_builds", ctypes.c_int), ("s_squared", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 def library_path() -> str:
     return _build.LIB_PATH
 
@@ -72,6 +94,15 @@ def lib():
         L.hfg_stream.argtypes = [vp]
         L.hfg_stream.restype = vp
         L.hfg_version.restype = ctypes.c_char_p
+        dpp = ctypes.POINTER(ctypes.c_double)
+        L.hfg_one_electron.argtypes = [ctypes.POINTER(_Basis), ip, ctypes.POINTER(ctypes.c_int), dpp, dpp, dpp, dpp]
+        L.hfg_scf_default_options.argtypes = [ctypes.POINTER(ScfOptions), ip]
+        L.hfg_scf_default_options.restype = None
+        L.hfg_scf_run.argtypes = [vp, ctypes.POINTER(ScfOptions), ip, ctypes.POINTER(ctypes.c_int), dpp, ip, ip,
+                                  ctypes.POINTER(ScfResult), dpp, dpp]
+        L.hfg_core_guess.argtypes = [vp, ctypes.POINTER(ScfOptions), ip, ctypes.POINTER(ctypes.c_int), dpp, ip, ip,
+                                     dpp, dpp]
+        L.hfg_measure_fma_peak.argtypes = [ip, ip, dpp]
         _lib = L
     return _lib
 
@@ -186,9 +217,74 @@ class Engine:
                                         ctypes.byref(cnt)))
         return out
 
+    def _opts(self, opts: dict, multiplicity: int) -> ScfOptions:
+        o = ScfOptions()
+        lib().hfg_scf_default_options(ctypes.byref(o), multiplicity)
+        for k, v in (opts or {}).items():
+            setattr(o, k, v)
+        return o
+
+    def scf(self, Z, xyz, charge=0, multiplicity=1, opts: dict | None = None):
+        """Full direct SCF on this engine's molecule; returns (result dict, Da, Db)."""
+        o = self._opts(opts, multiplicity)
+        Zc = np.ascontiguousarray(Z, dtype=np.int32)
+        X = np.ascontiguousarray(xyz, dtype=np.float64)
+        n = self.nao
+        Da, Db = np.zeros((n, n), order="F"), np.zeros((n, n), order="F")
+        r = ScfResult()
+        self._check(lib().hfg_scf_run(self.h, ctypes.byref(o), len(Zc), Zc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                      _dp(X), charge, multiplicity, ctypes.byref(r), _dp(Da), _dp(Db)))
+        return r.as_dict(), Da, Db
+
+    def core_guess(self, Z, xyz, charge=0, multiplicity=1, opts: dict | None = None):
+        o = self._opts(opts, multiplicity)
+        Zc = np.ascontiguousarray(Z, dtype=np.int32)
+        X = np.ascontiguousarray(xyz, dtype=np.float64)
+        n = self.nao
+        Da, Db = np.zeros((n, n), order="F"), np.zeros((n, n), order="F")
+        self._check(lib().hfg_core_guess(self.h, ctypes.byref(o), len(Zc), Zc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                         _dp(X), charge, multiplicity, _dp(Da), _dp(Db)))
+        return Da, Db
+
     def eri_block(self, a, b, c, d):
         ls = self._keep[0].a["l"]
         n = [(int(ls[s]) + 1) * (int(ls[s]) + 2) // 2 for s in (a, b, c, d)]
         out = np.zeros(int(np.prod(n)))
         self._check(lib().hfg_eri_block(self.h, a, b, c, d, _dp(out)))
         return out.reshape(n)
+
+
+def one_electron(soa: dict, Z, xyz):
+    """(S, T, V) host FP64 through hfg_one_electron."""
+    k = _BasisKeep(soa)
+    n = k.nao
+    S, T, V = (np.zeros((n, n), order="F") for _ in range(3))
+    Zc = np.ascontiguousarray(Z, dtype=np.int32)
+    X = np.ascontiguousarray(xyz, dtype=np.float64)
+    rc = lib().hfg_one_electron(ctypes.byref(k.s), len(Zc), Zc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(X),
+                                _dp(S), _dp(T), _dp(V))
+    if rc != HFG_OK:
+        raise HfgError(rc, "hfg_one_electron failed")
+    return S, T, V
+
+
+def measure_fma_peak(fp64: bool, device: int = 0) -> float:
+    """TFLOP/s of a register-only FMA loop on this GPU (FP64 or FP32 CUDA cores)."""
+    t = ctypes.c_double()
+    rc = lib().hfg_measure_fma_peak(device, 1 if fp64 else 0, ctypes.byref(t))
+    if rc != HFG_OK:
+        raise HfgError(rc, "hfg_measure_fma_peak failed")
+    return t.value
+
+
+def run_input(text: str, precision: int = FP64, fp32_cutoff: float = 1e-6, full_rebuild_every: int = 0,
+              basis_dir: str | None = None, device: int = 0):
+    """Runs a reference-format input end to end: parse, pack the basis, GPU direct SCF."""
+    from . import basis as _basis, inputs as _inputs
+
+    job = _inputs.parse(text)
+    soa = _basis.pack(job.basis, job.Z, job.xyz, basis_dir)
+    eng = Engine(soa, device=device)
+    opts = _inputs.scf_options(job, precision, fp32_cutoff, full_rebuild_every)
+    res, Da, Db = eng.scf(job.Z, job.xyz, job.charge, job.multiplicity, opts)
+    return res, Da, Db, eng

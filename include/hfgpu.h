@@ -130,6 +130,71 @@ int hfg_eri_block(hfg_engine* engine, int a, int b, int c, int d, double* out);
 /* The CUDA stream the engine launches on (a cudaStream_t), for callers that time or order work. */
 void* hfg_stream(hfg_engine* engine);
 
+/* ---------------------------------------------------------------------------------------------
+ * Host side of the SCF (the reference's SCF driver semantics, src/SCF.cpp:23-231 and 747-835),
+ * so that a caller can run a whole direct SCF with the GPU Fock build.
+ * ------------------------------------------------------------------------------------------- */
+
+/* IntegralEngine::overlapMatrix / kineticMatrix / nuclearAttractionMatrix (src/IntegralEngine.cpp:78-368):
+ * S, T, V (FP64, host, column-major nao x nao) for the basis and nuclei Z at xyz (bohr). */
+int hfg_one_electron(const hfg_basis* basis, int natom, const int* Z, const double* xyz, double* S, double* T,
+                     double* V);
+
+/* SCFOptions (include/SCF.hpp:9-32) plus the engine's own knobs. */
+typedef struct hfg_scf_options
+{
+    int max_iter;              /* MAX_ITER (30) */
+    double energy_tol;         /* ENERGY_TOL (1e-6) */
+    double density_tol;        /* DENSITY_TOL (1e-6), Frobenius norm of dD_tot */
+    int use_diis;              /* DIIS (1) */
+    int diis_size;             /* DIIS_SIZE (6) */
+    double diis_tol;           /* DIIS_TOL (1e-6) */
+    int unrestricted;          /* UNRESTRICTED (multiplicity != 1) */
+    int guess_mix;             /* GUESS_MIX (0) */
+    int damp;                  /* DAMP percentage (0) */
+    int max_damp_iter;         /* MAX_DAMP_CYCLES (= max_iter) */
+    double stop_damp_thresh;   /* STOP_DAMP_THRESH (0) */
+    double level_shift;        /* LEVEL_SHIFT (0) */
+    double lshift_gap_tol;     /* LSHIFT_GAP_TOL (infinity) */
+    double max_lshift_iter;    /* MAX_LSHIFT_CYCLES (= max_iter) */
+    double stop_lshift_thresh; /* STOP_LSHIFT_THRESH (0) */
+    double schwartz_threshold; /* SCHWARTZ_THRESH (1e-10) */
+    double density_threshold;  /* DENSITY_THRESH (1e-10) */
+    int precision;             /* HFG_PRECISION_FP64 / HFG_PRECISION_MIXED */
+    double fp32_cutoff;        /* FP32 cutoff of the mixed mode (1e-6) */
+    int full_rebuild_every;    /* 0: incremental builds as the reference; k > 0: full build every k iterations */
+    int verbose;               /* print the iteration table to stdout */
+} hfg_scf_options;
+
+typedef struct hfg_scf_result
+{
+    double e_electronic, e_nuclear, e_total;
+    int iterations; /* SCF cycles run (the reference's final iteration index + 1) */
+    int converged;
+    double delta_e, delta_d, diis_error;
+    double ms_total; /* wall time of the SCF (host clock), including the Fock builds */
+    double ms_fock;  /* device time of the Fock builds */
+    int fock_builds;
+    double s_squared; /* <S^2> (UHF) */
+} hfg_scf_result;
+
+/* The reference's defaults (SCF.hpp:9-32, Input.cpp:127-140) for a molecule of this multiplicity. */
+void hfg_scf_default_options(hfg_scf_options* opt, int multiplicity);
+
+/* SCF::SCF + SCF::run (src/SCF.cpp:13-135) for the single molecule of `engine`, whose nuclei are Z at xyz
+ * (bohr, the basis centres' atoms) with total charge and multiplicity.  Density matrices of the last
+ * iteration are written to D_alpha / D_beta (host, may be NULL). */
+int hfg_scf_run(hfg_engine* engine, const hfg_scf_options* opt, int natom, const int* Z, const double* xyz,
+                int charge, int multiplicity, hfg_scf_result* result, double* D_alpha, double* D_beta);
+
+/* Core-Hamiltonian guess densities (src/SCF.cpp:165-231), host output. */
+int hfg_core_guess(hfg_engine* engine, const hfg_scf_options* opt, int natom, const int* Z, const double* xyz,
+                   int charge, int multiplicity, double* D_alpha, double* D_beta);
+
+/* Peak FMA throughput of this GPU measured by a register-only FMA loop (TFLOP/s, FP64 if fp64 != 0,
+ * else FP32): the denominator of the ERI kernels' roofline. */
+int hfg_measure_fma_peak(int device, int fp64, double* tflops);
+
 /* Library version string. */
 const char* hfg_version(void);
 

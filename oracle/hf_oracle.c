@@ -13,6 +13,8 @@
  *   orc_schwartz             schwartzScreeningMatrix            src/IntegralEngine.cpp:695-728
  *   orc_fock_direct          SCF::buildFockMatrixDirect         src/SCF.cpp:523-744 (J/K part, no F_prev)
  *   orc_survivors            the screening predicates of        src/SCF.cpp:592-623
+ *   orc_fock_direct_sample   the same build over a sample of bra shell pairs (CPU-baseline timing)
+ *   orc_count_survivors      the number of quartets passing those predicates (to scale a sample)
  *   orc_one_electron         overlap/kinetic/nuclearAttraction  src/IntegralEngine.cpp:78-368
  *
  * The basis arrives as the structure of arrays that IntegralEngine builds (IntegralEngine.cpp:13-75):
@@ -511,6 +513,82 @@ long orc_survivors(const orc_basis* B, const double* Q, const double* dDtot, con
  * the reference ERI block, the AO-level |eri| < schwartz_thr skip, the symmetry-factor digestion
  * into the upper triangle, then the upper triangle mirrored.  Matrices are column-major n x n.
  * Returns the number of surviving shell quartets. */
+/* Digestion of one ERI block into thread-local J/K (SCF.cpp:637-711): each canonical AO quartet
+ * (ij|kl), i>=j, k>=l, ij>=kl, adds its distinct permutations into the upper triangle (row <= column). */
+static void digest_block(const orc_basis* B, long a, long b, long c, long d, const double* G, const double* dDtot,
+                         const double* dDa, const double* dDb, double sthr, double* Jp, double* Kap, double* Kbp)
+{
+    const size_t N = (size_t)B->nao;
+    const int na = nao_of(B->l[a]), nb = nao_of(B->l[b]), nc = nao_of(B->l[c]), nd = nao_of(B->l[d]);
+    for (int A = 0; A < na; ++A)
+    {
+        const size_t i = A + B->ao_off[a];
+        for (int Bq = 0; Bq < nb; ++Bq)
+        {
+            const size_t j = Bq + B->ao_off[b];
+            if (j > i)
+                continue;
+            for (int C = 0; C < nc; ++C)
+            {
+                const size_t k = C + B->ao_off[c];
+                const size_t lmax = (i == k) ? j : k;
+                for (int Dq = 0; Dq < nd; ++Dq)
+                {
+                    const size_t l = Dq + B->ao_off[d];
+                    if (l > lmax)
+                        continue;
+                    const double eri = G[((A * nb + Bq) * nc + C) * nd + Dq];
+                    if (fabs(eri) < sthr)
+                        continue;
+                    const size_t ji = j + i * N, lk = l + k * N, li = l + i * N, kj = k + j * N;
+                    const size_t lj = l + j * N, ki = k + i * N;
+                    const double f_kl = (k == l) ? 1.0 : 2.0, f_ij = (i == j) ? 1.0 : 2.0;
+                    Jp[ji] += f_kl * dDtot[lk] * eri;
+                    Jp[lk] += ((l != j || k != i) ? 1.0 : 0.0) * f_ij * dDtot[ji] * eri;
+                    const double f_jk = (j == k) ? 2.0 : 1.0;
+                    const double f_jl = (j == l && i != k) ? 2.0 : 1.0;
+                    const double f_ik = (i == k && j != l) ? 2.0 : 1.0;
+                    const size_t x1 = i < k ? i + k * N : ki;
+                    const size_t x2 = j < l ? j + l * N : lj;
+                    const size_t x3 = j < k ? j + k * N : kj;
+                    const double w1 = (x1 != li) ? f_ik : 0.0;
+                    const double w2 = (x2 != li && x2 != x1) ? f_jl : 0.0;
+                    const double w3 = (x3 != li && x3 != x1 && x3 != x2) ? f_jk : 0.0;
+                    Kap[li] += dDa[kj] * eri;
+                    Kap[x1] += w1 * dDa[lj] * eri;
+                    Kap[x2] += w2 * dDa[ki] * eri;
+                    Kap[x3] += w3 * dDa[li] * eri;
+                    if (Kbp)
+                    {
+                        Kbp[li] += dDb[kj] * eri;
+                        Kbp[x1] += w1 * dDb[lj] * eri;
+                        Kbp[x2] += w2 * dDb[ki] * eri;
+                        Kbp[x3] += w3 * dDb[li] * eri;
+                    }
+                }
+            }
+        }
+    }
+}
+
+static void mirror_upper(size_t N, double* J, double* Ka, double* Kb)
+{
+    /* selfadjointView<Upper>: mirror the upper triangle (row <= column) into the lower one. */
+    for (size_t c = 0; c < N; ++c)
+        for (size_t r = c + 1; r < N; ++r)
+        {
+            J[r + c * N] = J[c + r * N];
+            Ka[r + c * N] = Ka[c + r * N];
+            if (Kb)
+                Kb[r + c * N] = Kb[c + r * N];
+        }
+}
+
+/* J[dD_tot], K_alpha[dD_alpha] (and K_beta[dD_beta] when dDb != NULL) as SCF::buildFockMatrixDirect
+ * forms them (SCF.cpp:523-728): canonical shell-quartet loop (collapse(4), dynamic 32) with Schwartz and
+ * density screening, the reference ERI block, the AO-level |eri| < schwartz_thr skip, the symmetry-factor
+ * digestion into thread-local upper triangles, a critical-section reduction, then the upper triangle
+ * mirrored.  Matrices are column-major n x n.  Returns the number of surviving shell quartets. */
 long orc_fock_direct(const orc_basis* B, const double* Q, const double* dDtot, const double* dDa, const double* dDb,
                      double sthr, double dthr, double* J, double* Ka, double* Kb)
 {
@@ -545,59 +623,8 @@ long orc_fock_direct(const orc_basis* B, const double* Q, const double* dDtot, c
             if (!quartet_survives(ns, Q, Mt, Ma, Mb, a, b, c, d, sthr, dthr))
                 continue;
             ++survivors;
-            const int na = nao_of(B->l[a]), nb = nao_of(B->l[b]), nc = nao_of(B->l[c]), nd = nao_of(B->l[d]);
             orc_eri(B, a, b, c, d, G);
-            /* Digestion of SCF.cpp:637-711: each canonical AO quartet (ij|kl), i>=j, k>=l, ij>=kl, adds its
-             * distinct permutations into the upper triangle (row <= column). */
-            for (int A = 0; A < na; ++A)
-            {
-                const size_t i = A + B->ao_off[a];
-                for (int Bq = 0; Bq < nb; ++Bq)
-                {
-                    const size_t j = Bq + B->ao_off[b];
-                    if (j > i)
-                        continue;
-                    for (int C = 0; C < nc; ++C)
-                    {
-                        const size_t k = C + B->ao_off[c];
-                        const size_t lmax = (i == k) ? j : k;
-                        for (int Dq = 0; Dq < nd; ++Dq)
-                        {
-                            const size_t l = Dq + B->ao_off[d];
-                            if (l > lmax)
-                                continue;
-                            const double eri = G[((A * nb + Bq) * nc + C) * nd + Dq];
-                            if (fabs(eri) < sthr)
-                                continue;
-                            const size_t ji = j + i * N, lk = l + k * N, li = l + i * N, kj = k + j * N;
-                            const size_t lj = l + j * N, ki = k + i * N;
-                            const double f_kl = (k == l) ? 1.0 : 2.0, f_ij = (i == j) ? 1.0 : 2.0;
-                            Jp[ji] += f_kl * dDtot[lk] * eri;
-                            Jp[lk] += ((l != j || k != i) ? 1.0 : 0.0) * f_ij * dDtot[ji] * eri;
-                            const double f_jk = (j == k) ? 2.0 : 1.0;
-                            const double f_jl = (j == l && i != k) ? 2.0 : 1.0;
-                            const double f_ik = (i == k && j != l) ? 2.0 : 1.0;
-                            const size_t x1 = i < k ? i + k * N : ki;
-                            const size_t x2 = j < l ? j + l * N : lj;
-                            const size_t x3 = j < k ? j + k * N : kj;
-                            const double w1 = (x1 != li) ? f_ik : 0.0;
-                            const double w2 = (x2 != li && x2 != x1) ? f_jl : 0.0;
-                            const double w3 = (x3 != li && x3 != x1 && x3 != x2) ? f_jk : 0.0;
-                            Kap[li] += dDa[kj] * eri;
-                            Kap[x1] += w1 * dDa[lj] * eri;
-                            Kap[x2] += w2 * dDa[ki] * eri;
-                            Kap[x3] += w3 * dDa[li] * eri;
-                            if (Kbp)
-                            {
-                                Kbp[li] += dDb[kj] * eri;
-                                Kbp[x1] += w1 * dDb[lj] * eri;
-                                Kbp[x2] += w2 * dDb[ki] * eri;
-                                Kbp[x3] += w3 * dDb[li] * eri;
-                            }
-                        }
-                    }
-                }
-            }
+            digest_block(B, a, b, c, d, G, dDtot, dDa, dDb, sthr, Jp, Kap, Kbp);
         }
 #pragma omp critical(orc_fock_reduce)
         {
@@ -613,19 +640,150 @@ long orc_fock_direct(const orc_basis* B, const double* Q, const double* dDtot, c
         free(Kap);
         free(Kbp);
     }
-    /* selfadjointView<Upper>: mirror the upper triangle (row <= column) into the lower one. */
-    for (size_t c = 0; c < N; ++c)
-        for (size_t r = c + 1; r < N; ++r)
-        {
-            J[r + c * N] = J[c + r * N];
-            Ka[r + c * N] = Ka[c + r * N];
-            if (Kb)
-                Kb[r + c * N] = Kb[c + r * N];
-        }
+    mirror_upper(N, J, Ka, Kb);
     free(Mt);
     free(Ma);
     free(Mb);
     return survivors;
+}
+
+/* The same build restricted to the canonical quartets whose bra pair (a >= b) is flagged in
+ * bra_mask[a*(a+1)/2 + b]: a bounded sample of one build, used to time the CPU baseline on workloads
+ * whose full build takes too long on a CPU.  Returns the surviving quartets evaluated. */
+long orc_fock_direct_sample(const orc_basis* B, const double* Q, const double* dDtot, const double* dDa,
+                            const double* dDb, double sthr, double dthr, const unsigned char* bra_mask, double* J,
+                            double* Ka, double* Kb)
+{
+    const int ns = B->nshells;
+    const size_t N = (size_t)B->nao;
+    double* Mt = (double*)malloc(sizeof(double) * ns * ns);
+    double* Ma = (double*)malloc(sizeof(double) * ns * ns);
+    double* Mb = dDb ? (double*)malloc(sizeof(double) * ns * ns) : NULL;
+    shell_max(B, dDtot, Mt);
+    shell_max(B, dDa, Ma);
+    if (Mb)
+        shell_max(B, dDb, Mb);
+    memset(J, 0, sizeof(double) * N * N);
+    memset(Ka, 0, sizeof(double) * N * N);
+    if (Kb)
+        memset(Kb, 0, sizeof(double) * N * N);
+    const long npairs = (long)ns * (ns + 1) / 2;
+    long nsel = 0;
+    for (long p = 0; p < npairs; ++p) nsel += bra_mask[p] ? 1 : 0;
+    long* sel = (long*)malloc(sizeof(long) * (nsel > 0 ? nsel : 1));
+    nsel = 0;
+    for (long p = 0; p < npairs; ++p)
+        if (bra_mask[p])
+            sel[nsel++] = p;
+    long survivors = 0;
+#pragma omp parallel reduction(+ : survivors)
+    {
+        double* Jp  = (double*)calloc(N * N, sizeof(double));
+        double* Kap = (double*)calloc(N * N, sizeof(double));
+        double* Kbp = Kb ? (double*)calloc(N * N, sizeof(double)) : NULL;
+        double G[ORC_MAX_NAO * ORC_MAX_NAO * ORC_MAX_NAO * ORC_MAX_NAO];
+#pragma omp for schedule(dynamic, 1) nowait
+        for (long s = 0; s < nsel; ++s)
+        {
+            const long ab = sel[s];
+            long a = 0;
+            while ((a + 1) * (a + 2) / 2 <= ab) ++a;
+            const long b = ab - a * (a + 1) / 2;
+            for (long cd = 0; cd <= ab; ++cd)
+            {
+                long c = 0;
+                while ((c + 1) * (c + 2) / 2 <= cd) ++c;
+                const long d = cd - c * (c + 1) / 2;
+                if (!quartet_survives(ns, Q, Mt, Ma, Mb, a, b, c, d, sthr, dthr))
+                    continue;
+                ++survivors;
+                orc_eri(B, a, b, c, d, G);
+                digest_block(B, a, b, c, d, G, dDtot, dDa, dDb, sthr, Jp, Kap, Kbp);
+            }
+        }
+#pragma omp critical(orc_fock_reduce_sample)
+        {
+            for (size_t x = 0; x < N * N; ++x)
+            {
+                J[x] += Jp[x];
+                Ka[x] += Kap[x];
+                if (Kb)
+                    Kb[x] += Kbp[x];
+            }
+        }
+        free(Jp);
+        free(Kap);
+        free(Kbp);
+    }
+    mirror_upper(N, J, Ka, Kb);
+    free(sel);
+    free(Mt);
+    free(Ma);
+    free(Mb);
+    return survivors;
+}
+
+
+/* Number of canonical quartets surviving the predicates of SCF.cpp:602-623, without the O(nshells^4)
+ * scan: pairs sorted by Q descending, for each bra pair only the ket pairs of the Schwartz prefix are
+ * tested.  Used to scale a sampled CPU build to the full build. */
+static const double* g_sortQ;
+static int cmp_q_desc(const void* x, const void* y)
+{
+    const double a = g_sortQ[*(const long*)x], b = g_sortQ[*(const long*)y];
+    return a > b ? -1 : (a < b ? 1 : 0);
+}
+
+long orc_count_survivors(const orc_basis* B, const double* Q, const double* dDtot, const double* dDa, const double* dDb,
+                         double sthr, double dthr)
+{
+    const int ns = B->nshells;
+    const long np = (long)ns * (ns + 1) / 2;
+    long* ord = (long*)malloc(sizeof(long) * np);
+    double* qp = (double*)malloc(sizeof(double) * np);
+    int* pa = (int*)malloc(sizeof(int) * np);
+    int* pb = (int*)malloc(sizeof(int) * np);
+    long k = 0;
+    for (int a = 0; a < ns; ++a)
+        for (int b = 0; b <= a; ++b, ++k)
+        {
+            pa[k] = a;
+            pb[k] = b;
+            qp[k] = Q[a + (size_t)b * ns];
+            ord[k] = k;
+        }
+    g_sortQ = qp;
+    qsort(ord, (size_t)np, sizeof(long), cmp_q_desc);
+    double* Mt = (double*)malloc(sizeof(double) * ns * ns);
+    double* Ma = (double*)malloc(sizeof(double) * ns * ns);
+    double* Mb = dDb ? (double*)malloc(sizeof(double) * ns * ns) : NULL;
+    shell_max(B, dDtot, Mt);
+    shell_max(B, dDa, Ma);
+    if (Mb)
+        shell_max(B, dDb, Mb);
+    long total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (long i = 0; i < np; ++i)
+    {
+        const long pi = ord[i];
+        for (long j = 0; j <= i; ++j)
+        {
+            const long pj = ord[j];
+            if (qp[pi] * qp[pj] < sthr)
+                break;
+            /* canonical orientation is irrelevant for the predicate (it is symmetric) */
+            if (quartet_survives(ns, Q, Mt, Ma, Mb, pa[pi], pb[pi], pa[pj], pb[pj], sthr, dthr))
+                ++total;
+        }
+    }
+    free(ord);
+    free(qp);
+    free(pa);
+    free(pb);
+    free(Mt);
+    free(Ma);
+    free(Mb);
+    return total;
 }
 
 /* ------------------------------------------------------------------------------------------------

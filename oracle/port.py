@@ -48,6 +48,11 @@ def lib():
         L.orc_survivors.restype = ctypes.c_long
         L.orc_fock_direct.argtypes = [bp, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp, dp, dp]
         L.orc_fock_direct.restype = ctypes.c_long
+        L.orc_fock_direct_sample.argtypes = [bp, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double,
+                                             ctypes.POINTER(ctypes.c_ubyte), dp, dp, dp]
+        L.orc_fock_direct_sample.restype = ctypes.c_long
+        L.orc_count_survivors.argtypes = [bp, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double]
+        L.orc_count_survivors.restype = ctypes.c_long
         L.orc_one_electron.argtypes = [bp, ctypes.c_int, ip, dp, dp, dp, dp]
         L.orc_num_threads.restype = ctypes.c_int
         _lib = L
@@ -106,6 +111,21 @@ class Basis:
         args = [np.asfortranarray(x) if x is not None else None for x in (Q, dDtot, dDa, dDb)]
         ns = lib().orc_fock_direct(ctypes.byref(self.s), *[_dp(x) for x in args], sthr, dthr, _dp(J), _dp(Ka), _dp(Kb))
         return J, Ka, Kb, ns
+
+    def fock_direct_sample(self, Q, dDtot, dDa, bra_mask, dDb=None, sthr=1e-10, dthr=1e-10):
+        """The build restricted to bra pairs flagged in bra_mask (length nshells*(nshells+1)/2)."""
+        N = self.nao
+        J, Ka = np.zeros((N, N), order="F"), np.zeros((N, N), order="F")
+        Kb = np.zeros((N, N), order="F") if dDb is not None else None
+        args = [np.asfortranarray(x) if x is not None else None for x in (Q, dDtot, dDa, dDb)]
+        m = np.ascontiguousarray(bra_mask, dtype=np.uint8)
+        n = lib().orc_fock_direct_sample(ctypes.byref(self.s), *[_dp(x) for x in args], sthr, dthr,
+                                         m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), _dp(J), _dp(Ka), _dp(Kb))
+        return J, Ka, Kb, n
+
+    def count_survivors(self, Q, dDtot, dDa, dDb=None, sthr=1e-10, dthr=1e-10):
+        args = [np.asfortranarray(x) if x is not None else None for x in (Q, dDtot, dDa, dDb)]
+        return lib().orc_count_survivors(ctypes.byref(self.s), *[_dp(x) for x in args], sthr, dthr)
 
     def one_electron(self, Z, xyz):
         N = self.nao

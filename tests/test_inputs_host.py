@@ -1,0 +1,52 @@
+"""Host-side pieces that need no GPU: the input reader and the FP64 one-electron integrals."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+
+def test_parse_reference_example():
+    from hfgpu import inputs
+
+    text = """$molecule    # H2O molecule
+    0    1
+    H    1.4327076887   -0.9610871670    0.0000000000
+    H   -1.4327076887   -0.9610871670    0.0000000000
+    O   -0.0000000000    0.2403536480   -0.0000000000
+$end
+$scf
+    UNRESTRICTED       TRUE
+    GUESS_MIX          2      # break symmetry
+    MAX_ITER           50
+    ENERGY_TOL         1.0e-8
+    DIRECT             TRUE
+    DENSITY_THRESH     1.0e-8
+    PRINT_FULL_MOS     true
+$end
+$basis
+    6-31G
+$end
+"""
+    job = inputs.parse(text)
+    assert job.Z == [1, 1, 8] and job.charge == 0 and job.multiplicity == 1 and job.basis == "6-31G"
+    o = inputs.scf_options(job)
+    assert o["unrestricted"] == 1 and o["guess_mix"] == 2 and o["max_iter"] == 50
+    assert o["max_damp_iter"] == 50 and o["energy_tol"] == 1e-8 and o["density_threshold"] == 1e-8
+
+
+def test_parse_rejects_unknown_keyword():
+    from hfgpu import inputs
+
+    with pytest.raises(ValueError):
+        inputs.parse("$molecule\n0 1\nH 0 0 0\n$end\n$scf\nFOO 1\n$end\n$basis\nsto-3g\n$end\n")
+
+
+@pytest.mark.parametrize("name", ["h2o_631g", "w2_631gss", "w2_ccpvdz"])
+def test_one_electron_matches_reference(name):
+    from hfgpu import build, engine
+
+    build.build(verbose=False)
+    g = load_golden(name)
+    S, T, V = engine.one_electron(g["soa"], g["Z"], g["xyz"])
+    for a, b in ((S, g["S"]), (T, g["T"]), (V, g["V"])):
+        assert np.max(np.abs(a - b)) <= 1e-11 * max(1.0, np.abs(b).max())
