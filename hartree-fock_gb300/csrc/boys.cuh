@@ -82,7 +82,24 @@ template <typename Real> std::vector<Real> boys_slice_host(int L)
     return out;
 }
 
+// 1/k! for the e^x series.
+__host__ __device__ constexpr double inv_fact(int k)
+{
+    double f = 1.0;
+    for (int i = 2; i <= k; ++i) f *= i;
+    return 1.0 / f;
+}
+// y = t + magic rounds t to an integer held in the low bits of y: 1.5 * 2^52 (double), 1.5 * 2^23 (float).
+template <typename Real> constexpr double kRoundMagic = 0.0;
+template <> constexpr double kRoundMagic<double> = 6755399441055744.0;
+template <> constexpr double kRoundMagic<float>  = 12582912.0;
+template <typename Real> constexpr int kRoundMagicLow = 0;
+template <> constexpr int kRoundMagicLow<double> = 0;          // low 32 bits of 1.5*2^52 are zero
+template <> constexpr int kRoundMagicLow<float>  = 0x400000;   // mantissa of 1.5*2^23
+
 #ifdef __CUDACC__
+__device__ __forceinline__ int bits_low(double y) { return __double2loint(y); }
+__device__ __forceinline__ int bits_low(float y) { return __float_as_int(y) & 0x7fffff; }
 __device__ __forceinline__ double hfg_rsqrt(double x) { return rsqrt(x); }
 __device__ __forceinline__ float hfg_rsqrt(float x) { return rsqrtf(x); }
 
@@ -99,20 +116,22 @@ template <int L, typename Real> __device__ __forceinline__ void boys_eval(Real T
         for (int m = 0; m < L; ++m) F[m + 1] = (Real(m) + Real(0.5)) * invT * F[m];
         return;
     }
-    // T is finite and >= 0 for valid inputs; the clamp keeps a corrupt T inside the slice.
-    const int pt      = max(0, min(static_cast<int>(T * Real(G::kInvStep) + Real(0.5)), G::kPoints - 1));
-    const Real x      = Real(pt) * Real(G::kStep) - T; // -d
-    const Real* g     = slice + pt * G::kRow;
-    Real f            = g[G::kTerms - 1];
+    // Nearest grid point without a float->int conversion: adding 1.5*2^52 leaves round(T/h) in the low
+    // mantissa bits (T is finite and >= 0 here; the clamp keeps a corrupt T inside the slice).
+    const Real y  = T * Real(G::kInvStep) + Real(kRoundMagic<Real>);
+    const int pt  = max(0, min(static_cast<int>(bits_low(y) - kRoundMagicLow<Real>), G::kPoints - 1));
+    const Real x  = (y - Real(kRoundMagic<Real>)) * Real(G::kStep) - T; // T_i - T
+    const Real* g = slice + pt * G::kRow;
+    Real f        = g[G::kTerms - 1];
 #pragma unroll
     for (int k = G::kTerms - 2; k >= 0; --k) f = f * x + g[k];
     F[L] = f;
     if constexpr (L > 0)
     {
         // e^{-T} = e^{-T_i} * e^{x}, x = T_i - T, |x| <= h/2: series to the same order as the Taylor part.
-        Real ex = Real(1);
+        Real ex = Real(inv_fact(G::kTerms));
 #pragma unroll
-        for (int k = G::kTerms; k >= 1; --k) ex = ex * x * Real(1.0 / k) + Real(1);
+        for (int k = G::kTerms - 1; k >= 0; --k) ex = ex * x + Real(inv_fact(k));
         const Real e    = g[G::kTerms] * ex;
         const Real twoT = T + T;
 #pragma unroll

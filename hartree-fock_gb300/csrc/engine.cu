@@ -132,10 +132,16 @@ struct hfg_engine
     bool have_Q = false;
     std::vector<int> cls_ids[hfg::kNumPairClasses];
     std::vector<double> cls_Q[hfg::kNumPairClasses];
-    std::vector<int2> cls_rng[hfg::kNumPairClasses]; // per molecule [begin, end) in the class list
+    // Segments of equal primitive-pair count: x = begin, y = end (positions in the class list), z = npp.
+    std::vector<int4> cls_seg[hfg::kNumPairClasses];
+    std::vector<int2> cls_molseg[hfg::kNumPairClasses]; // per molecule: [first, end) segment
     hfg::DevBuf<int> d_cls_ids[hfg::kNumPairClasses];
     hfg::DevBuf<double> d_cls_Q[hfg::kNumPairClasses];
-    hfg::DevBuf<int2> d_cls_rng[hfg::kNumPairClasses];
+    hfg::DevBuf<int4> d_cls_seg[hfg::kNumPairClasses];
+    hfg::DevBuf<int2> d_cls_molseg[hfg::kNumPairClasses];
+    hfg::DevBuf<unsigned> d_bra_cnt[hfg::kNumQuartetClasses];            // per bra pair: survivors (fp64, fp32)
+    hfg::DevBuf<unsigned long long> d_bra_off[hfg::kNumQuartetClasses];  // per bra pair: list offsets
+    hfg::DevBuf<unsigned long long> d_scan_tmp;
 
     // Quartet lists (capacity for the Schwartz threshold they were sized for).
     double cap_thr = -1.0;
@@ -199,7 +205,8 @@ struct BuildArgs
     int n1;
     const int* ids2;
     const double* Q2;
-    const int2* rng2;
+    const int4* seg2;    // ket class segments (equal primitive-pair count, Q descending inside)
+    const int2* molseg2; // per molecule: ket segment range
     bool same_class;
     const PairRec* pairs;
     const double* Mt;
@@ -209,19 +216,23 @@ struct BuildArgs
     const int* nsh;
     double sthr, dthr, cutoff;
     int mixed;
+    int pass;                      // 0: count per bra pair, 1: write at the scanned offsets
+    unsigned* bra_cnt;             // [n1][2]
+    const unsigned long long* bra_off; // [n1][2] exclusive offsets (pass 1)
     Quartet* out64;
     Quartet* out32;
-    unsigned long long cap;
-    unsigned long long* cnt64;
-    unsigned long long* cnt32;
     unsigned long long* prim64;
     unsigned long long* prim32;
-    unsigned long long* overflow;
+    unsigned long long cap; // list capacity (the Schwartz-only count): writes beyond it are dropped
 };
 
-// Survival list of one quartet class: one warp per bra pair; candidate ket pairs are the Schwartz
-// prefix of the ket class list (sorted by Q descending, so Q_i*Q_j < thr holds from a point on), then
-// the density predicate of SCF.cpp:610-623.  FP32 / FP64 split by the quartet bound Q_i Q_j max|dD|.
+// Survival list of one quartet class in two deterministic passes, one warp per bra pair.  Ket
+// candidates are visited segment by segment (segments of equal primitive-pair count, Q descending
+// inside each), and inside a segment only the Schwartz prefix Q_i*Q_j >= thr is tested (the product is
+// monotone in Q_j); the density predicate is that of SCF.cpp:610-623.  Pass 0 counts survivors per
+// bra pair and precision, pass 1 writes them at scanned offsets in candidate order, so the list is
+// ordered by bra pair and, inside a bra pair, by ket primitive count: a warp of the class kernels sees
+// quartets of equal primitive counts.  FP32 / FP64 split by the quartet bound Q_i Q_j max|dD|.
 __global__ void build_lists_kernel(BuildArgs a)
 {
     const int lane = threadIdx.x & 31;
@@ -231,73 +242,149 @@ __global__ void build_lists_kernel(BuildArgs a)
     const int pid_i  = a.ids1[i];
     const double Qi  = a.Q1[i];
     const PairRec pi = a.pairs[pid_i];
-    const int2 r     = a.rng2[pi.mol];
-    const int jb     = r.x;
-    const int je     = a.same_class ? i + 1 : r.y;
-    int lo = jb, hi = je;
-    while (lo < hi)
-    {
-        const int mid = (lo + hi) >> 1;
-        if (Qi * a.Q2[mid] < a.sthr)
-            hi = mid;
-        else
-            lo = mid + 1;
-    }
-    const int jend = lo;
+    const int2 ms    = a.molseg2[pi.mol];
     const long long so = a.smax_off[pi.mol];
     const int ns = a.nsh[pi.mol];
     auto M = [&](const double* m, int x, int y) { return m[so + x + (long long)y * ns]; };
     const int sa = pi.sh1, sb = pi.sh2;
     const double dab = 2.0 * M(a.Mt, sa, sb);
-    for (int base = jb; base < jend; base += 32)
+    unsigned c64 = 0, c32 = 0;
+    unsigned long long p64 = 0, p32 = 0;
+    const unsigned long long o64 = a.pass ? a.bra_off[2 * i] : 0ull;
+    const unsigned long long o32 = a.pass ? a.bra_off[2 * i + 1] : 0ull;
+    for (int sidx = ms.x; sidx < ms.y; ++sidx)
     {
-        const int j = base + lane;
-        bool s64 = false, s32 = false;
-        int pid_j = 0;
-        unsigned long long prims = 0;
-        if (j < jend)
+        const int4 seg = a.seg2[sidx];
+        const int jb = seg.x;
+        const int je = a.same_class ? min(seg.y, i + 1) : seg.y;
+        if (jb >= je)
+            continue;
+        int lo = jb, hi = je;
+        while (lo < hi)
         {
-            pid_j = a.ids2[j];
-            const PairRec pj = a.pairs[pid_j];
-            const int sc = pj.sh1, sd = pj.sh2;
-            double md = fmax(fmax(dab, 2.0 * M(a.Mt, sc, sd)),
-                             fmax(fmax(M(a.Ma, sa, sc), M(a.Ma, sa, sd)), fmax(M(a.Ma, sb, sc), M(a.Ma, sb, sd))));
-            if (a.Mb)
-                md = fmax(md, fmax(fmax(M(a.Mb, sa, sc), M(a.Mb, sa, sd)), fmax(M(a.Mb, sb, sc), M(a.Mb, sb, sd))));
-            if (md >= a.dthr)
-            {
-                const bool lowp = a.mixed && (Qi * a.Q2[j] * md < a.cutoff);
-                s32 = lowp;
-                s64 = !lowp;
-                prims = (unsigned long long)pi.npp * pj.npp;
-            }
+            const int mid = (lo + hi) >> 1;
+            if (Qi * a.Q2[mid] < a.sthr)
+                hi = mid;
+            else
+                lo = mid + 1;
         }
-        for (int prec = 0; prec < 2; ++prec)
+        const int jend = lo;
+        for (int base = jb; base < jend; base += 32)
         {
-            const bool mine = prec == 0 ? s64 : s32;
-            const unsigned mask = __ballot_sync(0xffffffffu, mine);
-            if (mask == 0)
-                continue;
-            unsigned long long* cnt = prec == 0 ? a.cnt64 : a.cnt32;
-            unsigned long long slot = 0;
-            const int leader = __ffs(mask) - 1;
-            if (lane == leader)
-                slot = atomicAdd(cnt, (unsigned long long)__popc(mask));
-            slot = __shfl_sync(0xffffffffu, slot, leader);
-            unsigned long long pr = mine ? prims : 0ull;
-            for (int o = 16; o > 0; o >>= 1) pr += __shfl_down_sync(0xffffffffu, pr, o);
-            if (lane == 0)
-                atomicAdd(prec == 0 ? a.prim64 : a.prim32, pr);
-            if (mine)
+            const int j = base + lane;
+            bool s64 = false, s32 = false;
+            int pid_j = 0;
+            if (j < jend)
             {
-                const unsigned long long pos = slot + __popc(mask & ((1u << lane) - 1u));
-                Quartet* out = prec == 0 ? a.out64 : a.out32;
-                if (pos < a.cap)
-                    out[pos] = Quartet {static_cast<uint32_t>(pid_i), static_cast<uint32_t>(pid_j)};
-                else
-                    atomicAdd(a.overflow, 1ull);
+                pid_j = a.ids2[j];
+                const PairRec pj = a.pairs[pid_j];
+                const int sc = pj.sh1, sd = pj.sh2;
+                double md = fmax(fmax(dab, 2.0 * M(a.Mt, sc, sd)),
+                                 fmax(fmax(M(a.Ma, sa, sc), M(a.Ma, sa, sd)), fmax(M(a.Ma, sb, sc), M(a.Ma, sb, sd))));
+                if (a.Mb)
+                    md = fmax(md, fmax(fmax(M(a.Mb, sa, sc), M(a.Mb, sa, sd)), fmax(M(a.Mb, sb, sc), M(a.Mb, sb, sd))));
+                if (md >= a.dthr)
+                {
+                    const bool lowp = a.mixed && (Qi * a.Q2[j] * md < a.cutoff);
+                    s32 = lowp;
+                    s64 = !lowp;
+                }
             }
+            const unsigned m64 = __ballot_sync(0xffffffffu, s64);
+            const unsigned m32 = __ballot_sync(0xffffffffu, s32);
+            const unsigned lt  = (1u << lane) - 1u;
+            if (a.pass)
+            {
+                const Quartet qv {static_cast<uint32_t>(pid_i), static_cast<uint32_t>(pid_j)};
+                const unsigned long long w64 = o64 + c64 + __popc(m64 & lt), w32 = o32 + c32 + __popc(m32 & lt);
+                if (s64 && w64 < a.cap)
+                    a.out64[w64] = qv;
+                if (s32 && w32 < a.cap)
+                    a.out32[w32] = qv;
+            }
+            c64 += __popc(m64);
+            c32 += __popc(m32);
+            const unsigned long long pp = (unsigned long long)pi.npp * seg.z;
+            p64 += pp * __popc(m64);
+            p32 += pp * __popc(m32);
         }
+    }
+    if (a.pass == 0 && lane == 0)
+    {
+        a.bra_cnt[2 * i]     = c64;
+        a.bra_cnt[2 * i + 1] = c32;
+        if (p64)
+            atomicAdd(a.prim64, p64);
+        if (p32)
+            atomicAdd(a.prim32, p32);
+    }
+}
+
+// Exclusive scan of the per-bra counts (two interleaved sequences, fp64 and fp32) in three steps:
+// per-block scan, scan of the block totals (one block), add the block offsets.  The grand totals land
+// in total[0..1] (the class kernels' list lengths).
+constexpr int kScanBlock = 1024;
+__global__ void scan_block_kernel(const unsigned* __restrict__ cnt, unsigned long long* __restrict__ off, int n,
+                                  unsigned long long* __restrict__ block_tot)
+{
+    __shared__ unsigned long long warp_tot[2][32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = 0; q < 2; ++q)
+    {
+        unsigned long long v = i < n ? cnt[2 * i + q] : 0ull, x = v;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o)
+                x += y;
+        }
+        if (lane == 31)
+            warp_tot[q][w] = x;
+        __syncthreads();
+        if (w == 0)
+        {
+            unsigned long long t = warp_tot[q][lane], tx = t;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, tx, o);
+                if (lane >= o)
+                    tx += y;
+            }
+            warp_tot[q][lane] = tx - t; // exclusive warp offsets
+            if (lane == 31)
+                block_tot[2 * blockIdx.x + q] = tx;
+        }
+        __syncthreads();
+        if (i < n)
+            off[2 * i + q] = x - v + warp_tot[q][w];
+        __syncthreads();
+    }
+}
+
+__global__ void scan_tops_kernel(unsigned long long* __restrict__ block_tot, int nb, unsigned long long* __restrict__ total)
+{
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 2; ++q)
+        {
+            unsigned long long run = 0;
+            for (int b = 0; b < nb; ++b)
+            {
+                const unsigned long long t = block_tot[2 * b + q];
+                block_tot[2 * b + q] = run;
+                run += t;
+            }
+            total[q] = run;
+        }
+}
+
+__global__ void scan_add_kernel(unsigned long long* __restrict__ off, int n, const unsigned long long* __restrict__ block_tot)
+{
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n)
+    {
+        off[2 * i] += block_tot[2 * blockIdx.x];
+        off[2 * i + 1] += block_tot[2 * blockIdx.x + 1];
     }
 }
 
@@ -502,12 +589,12 @@ static void pack_molecules(hfg_engine* e)
                                           b.coeff[b.prim_off[bb] + pb] * b.radial[b.prim_off[a] + pa] *
                                           b.radial[b.prim_off[bb] + pb];
                         std::vector<double> rec(stride, 0.0);
-                        rec[0] = ip;
-                        rec[1] = p;
-                        rec[2] = P[0];
-                        rec[3] = P[1];
-                        rec[4] = P[2];
-                        rec[5] = Kw;
+                        rec[0] = p;
+                        rec[1] = P[0];
+                        rec[2] = P[1];
+                        rec[3] = P[2];
+                        rec[4] = std::sqrt(kTwoPi25) * ip * Kw;
+                        rec[5] = ip;
                         double E[3][kMaxL + 1][kMaxL + 1][2 * kMaxL + 1];
                         for (int k = 0; k < 3; ++k) hermite_1d(l1, l2, p, PA[k], PB[k], E[k]);
                         int x = kPairHeader;
@@ -640,7 +727,8 @@ static void compute_schwartz(hfg_engine* e)
     e->d_store.release();
 }
 
-// Sorts each pair class by (molecule, Q descending) and uploads the class lists.
+// Sorts each pair class by (molecule, primitive-pair count descending, Q descending) and records the
+// segments of equal primitive-pair count; uploads the class lists.
 static void sort_classes(hfg_engine* e)
 {
     for (int pc = 0; pc < kNumPairClasses; ++pc)
@@ -651,27 +739,56 @@ static void sort_classes(hfg_engine* e)
             if (e->pair_class_of[k] == pc)
                 ids.push_back(static_cast<int>(k));
         std::stable_sort(ids.begin(), ids.end(), [&](int x, int y) {
-            if (e->pairs[x].mol != e->pairs[y].mol)
-                return e->pairs[x].mol < e->pairs[y].mol;
+            const PairRec &px = e->pairs[x], &py = e->pairs[y];
+            if (px.mol != py.mol)
+                return px.mol < py.mol;
+            if (px.npp != py.npp)
+                return px.npp > py.npp;
             return e->Qpair[x] > e->Qpair[y];
         });
         e->cls_Q[pc].resize(ids.size());
         for (size_t k = 0; k < ids.size(); ++k) e->cls_Q[pc][k] = e->Qpair[ids[k]];
-        e->cls_rng[pc].assign(e->nmol, make_int2(0, 0));
+        e->cls_seg[pc].clear();
+        e->cls_molseg[pc].assign(e->nmol, make_int2(0, 0));
         size_t k = 0;
         for (int m = 0; m < e->nmol; ++m)
         {
-            const size_t b = k;
-            while (k < ids.size() && e->pairs[ids[k]].mol == m) ++k;
-            e->cls_rng[pc][m] = make_int2(static_cast<int>(b), static_cast<int>(k));
+            const int first = static_cast<int>(e->cls_seg[pc].size());
+            while (k < ids.size() && e->pairs[ids[k]].mol == m)
+            {
+                const size_t b = k;
+                const int npp  = e->pairs[ids[k]].npp;
+                while (k < ids.size() && e->pairs[ids[k]].mol == m && e->pairs[ids[k]].npp == npp) ++k;
+                e->cls_seg[pc].push_back(make_int4(static_cast<int>(b), static_cast<int>(k), npp, m));
+            }
+            e->cls_molseg[pc][m] = make_int2(first, static_cast<int>(e->cls_seg[pc].size()));
         }
         e->d_cls_ids[pc].upload(ids, e->stream);
         e->d_cls_Q[pc].upload(e->cls_Q[pc], e->stream);
-        e->d_cls_rng[pc].upload(e->cls_rng[pc], e->stream);
+        e->d_cls_seg[pc].upload(e->cls_seg[pc], e->stream);
+        e->d_cls_molseg[pc].upload(e->cls_molseg[pc], e->stream);
     }
     HFG_CUDA(cudaStreamSynchronize(e->stream));
     e->have_Q  = true;
     e->cap_thr = -1.0; // capacities depend on Q
+}
+
+// Schwartz prefix of bra position i (class P1) inside ket segment seg (class P2).
+static int prefix_end(const hfg_engine* e, int P1, int P2, size_t i, const int4& seg, double sthr)
+{
+    const int jb = seg.x;
+    const int je = (P1 == P2) ? std::min(seg.y, static_cast<int>(i) + 1) : seg.y;
+    int lo = jb, hi = std::max(jb, je);
+    const double Qi = e->cls_Q[P1][i];
+    while (lo < hi)
+    {
+        const int mid = (lo + hi) >> 1;
+        if (Qi * e->cls_Q[P2][mid] < sthr)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
 }
 
 // Exact Schwartz-only survivor count per quartet class (an upper bound of any build's list).
@@ -684,28 +801,22 @@ static void size_lists(hfg_engine* e, double sthr, bool mixed)
         {
             const int qc = quartet_class(P1, P2);
             unsigned long long c = 0;
-            const auto& Q1 = e->cls_Q[P1];
-            const auto& Q2 = e->cls_Q[P2];
-            for (size_t i = 0; i < Q1.size(); ++i)
+            for (size_t i = 0; i < e->cls_ids[P1].size(); ++i)
             {
                 const int mol = e->pairs[e->cls_ids[P1][i]].mol;
-                const int jb = e->cls_rng[P2][mol].x;
-                const int je = (P1 == P2) ? static_cast<int>(i) + 1 : e->cls_rng[P2][mol].y;
-                int lo = jb, hi = je;
-                while (lo < hi)
+                const int2 ms = e->cls_molseg[P2][mol];
+                for (int sg = ms.x; sg < ms.y; ++sg)
                 {
-                    const int mid = (lo + hi) >> 1;
-                    if (Q1[i] * Q2[mid] < sthr)
-                        hi = mid;
-                    else
-                        lo = mid + 1;
+                    const int4& seg = e->cls_seg[P2][sg];
+                    c += static_cast<unsigned long long>(std::max(0, prefix_end(e, P1, P2, i, seg, sthr) - seg.x));
                 }
-                c += static_cast<unsigned long long>(lo - jb);
             }
             e->cap[qc] = c;
             e->d_list[qc][0].alloc(std::max<unsigned long long>(c, 1));
             if (mixed)
                 e->d_list[qc][1].alloc(std::max<unsigned long long>(c, 1));
+            e->d_bra_cnt[qc].alloc(2 * std::max<size_t>(e->cls_ids[P1].size(), 1));
+            e->d_bra_off[qc].alloc(2 * std::max<size_t>(e->cls_ids[P1].size(), 1));
         }
     e->cap_thr   = sthr;
     e->cap_mixed = mixed;
@@ -764,55 +875,72 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
         HFG_CUDA(cudaGetLastError());
     }
 
-    // Lists.
+    // Lists: count pass, scan, write pass, per quartet class.
     const int ncnt = kNumQuartetClasses * 2;
     e->d_counts.alloc(2 * ncnt + 1);
     HFG_CUDA(cudaMemsetAsync(e->d_counts.p, 0, sizeof(unsigned long long) * (2 * ncnt + 1), s));
     int launches = nspin * (mixed ? 2 : 1) + nspin;
+    size_t max_blocks = 1;
     for (int P1 = 0; P1 < kNumPairClasses; ++P1)
-        for (int P2 = 0; P2 <= P1; ++P2)
-        {
-            const int qc = quartet_class(P1, P2);
-            if (e->cap[qc] == 0 || e->cls_ids[P1].empty() || e->cls_ids[P2].empty())
-                continue;
-            BuildArgs a {};
-            a.ids1 = e->d_cls_ids[P1].p;
-            a.Q1   = e->d_cls_Q[P1].p;
-            a.n1   = static_cast<int>(e->cls_ids[P1].size());
-            a.ids2 = e->d_cls_ids[P2].p;
-            a.Q2   = e->d_cls_Q[P2].p;
-            a.rng2 = e->d_cls_rng[P2].p;
-            a.same_class = P1 == P2;
-            a.pairs = e->d_pairs.p;
-            a.Mt = e->d_smax[0].p;
-            a.Ma = e->d_smax[1].p;
-            a.Mb = uhf ? e->d_smax[2].p : nullptr;
-            a.smax_off = e->d_smax_off.p;
-            a.nsh = e->d_nsh.p;
-            a.sthr = r.schwartz_threshold;
-            a.dthr = r.density_threshold;
-            a.cutoff = r.fp32_cutoff;
-            a.mixed = mixed ? 1 : 0;
-            a.out64 = e->d_list[qc][0].p;
-            a.out32 = mixed ? e->d_list[qc][1].p : nullptr;
-            a.cap = e->cap[qc];
-            a.cnt64 = e->d_counts.p + 2 * qc;
-            a.cnt32 = e->d_counts.p + 2 * qc + 1;
-            a.prim64 = e->d_counts.p + ncnt + 2 * qc;
-            a.prim32 = e->d_counts.p + ncnt + 2 * qc + 1;
-            a.overflow = e->d_counts.p + 2 * ncnt;
-            const long long threads = static_cast<long long>(a.n1) * 32;
-            build_lists_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, s>>>(a);
-            HFG_CUDA(cudaGetLastError());
-            ++launches;
-        }
+        max_blocks = std::max(max_blocks, (e->cls_ids[P1].size() + kScanBlock - 1) / kScanBlock);
+    e->d_scan_tmp.alloc(2 * max_blocks);
+    for (int pass = 0; pass < 2; ++pass)
+        for (int P1 = 0; P1 < kNumPairClasses; ++P1)
+            for (int P2 = 0; P2 <= P1; ++P2)
+            {
+                const int qc = quartet_class(P1, P2);
+                if (e->cap[qc] == 0 || e->cls_ids[P1].empty() || e->cls_ids[P2].empty())
+                    continue;
+                BuildArgs a {};
+                a.ids1 = e->d_cls_ids[P1].p;
+                a.Q1   = e->d_cls_Q[P1].p;
+                a.n1   = static_cast<int>(e->cls_ids[P1].size());
+                a.ids2 = e->d_cls_ids[P2].p;
+                a.Q2   = e->d_cls_Q[P2].p;
+                a.seg2 = e->d_cls_seg[P2].p;
+                a.molseg2 = e->d_cls_molseg[P2].p;
+                a.same_class = P1 == P2;
+                a.pairs = e->d_pairs.p;
+                a.Mt = e->d_smax[0].p;
+                a.Ma = e->d_smax[1].p;
+                a.Mb = uhf ? e->d_smax[2].p : nullptr;
+                a.smax_off = e->d_smax_off.p;
+                a.nsh = e->d_nsh.p;
+                a.sthr = r.schwartz_threshold;
+                a.dthr = r.density_threshold;
+                a.cutoff = r.fp32_cutoff;
+                a.mixed = mixed ? 1 : 0;
+                a.pass = pass;
+                a.bra_cnt = e->d_bra_cnt[qc].p;
+                a.bra_off = e->d_bra_off[qc].p;
+                a.out64 = e->d_list[qc][0].p;
+                a.out32 = mixed ? e->d_list[qc][1].p : nullptr;
+                a.prim64 = e->d_counts.p + ncnt + 2 * qc;
+                a.prim32 = e->d_counts.p + ncnt + 2 * qc + 1;
+                a.cap = e->cap[qc];
+                const long long threads = static_cast<long long>(a.n1) * 32;
+                build_lists_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, s>>>(a);
+                HFG_CUDA(cudaGetLastError());
+                ++launches;
+                if (pass == 0)
+                {
+                    const int nb = (a.n1 + kScanBlock - 1) / kScanBlock;
+                    scan_block_kernel<<<nb, kScanBlock, 0, s>>>(e->d_bra_cnt[qc].p, e->d_bra_off[qc].p, a.n1,
+                                                                e->d_scan_tmp.p);
+                    scan_tops_kernel<<<1, 32, 0, s>>>(e->d_scan_tmp.p, nb, e->d_counts.p + 2 * qc);
+                    scan_add_kernel<<<nb, kScanBlock, 0, s>>>(e->d_bra_off[qc].p, a.n1, e->d_scan_tmp.p);
+                    HFG_CUDA(cudaGetLastError());
+                    launches += 3;
+                }
+            }
     e->h_counts.assign(2 * ncnt + 1, 0);
     HFG_CUDA(cudaMemcpyAsync(e->h_counts.data(), e->d_counts.p, sizeof(unsigned long long) * (2 * ncnt + 1),
                              cudaMemcpyDeviceToHost, s));
     HFG_CUDA(cudaEventRecord(e->ev[2], s));
     HFG_CUDA(cudaStreamSynchronize(s));
-    if (e->h_counts[2 * ncnt] != 0)
-        throw HfgError(HFG_ERR_OVERFLOW, "fock: quartet list overflow");
+    for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+        if (e->h_counts[2 * qc] > e->cap[qc] || e->h_counts[2 * qc + 1] > e->cap[qc])
+            throw HfgError(HFG_ERR_OVERFLOW, "fock: quartet list overflow");
 
     // Class kernels: FP64 lists, then FP32 lists.
     for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
@@ -838,6 +966,7 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
             c.view.Ya    = e->d_acc[1].p;
             c.view.Yb    = e->d_acc[2].p;
             c.view.ao_thr = r.schwartz_threshold;
+            c.view.ao_thr_f = static_cast<float>(r.schwartz_threshold);
             c.boys_slice = prec == 1 ? static_cast<const void*>(e->d_boys32[L].p) : e->d_boys64[L].p;
             c.tables     = e->d_tables.p;
             c.fp32       = prec == 1;

@@ -47,6 +47,7 @@ struct FockView
     const long long* mat_off;           // per molecule: offset of its n x n block in the packed matrices
     const int* mat_ld;                  // per molecule: n
     double ao_thr;                      // AO-level skip threshold (SCHWARTZ_THRESH)
+    float ao_thr_f;                     // the same threshold for the FP32 kernels
     double* store;                      // if set: write the quartets' integrals here instead of digesting
 };
 
@@ -133,7 +134,7 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
     for (int ib = 0; ib < bra.npp; ++ib)
     {
         const Real* __restrict__ rb = tb + static_cast<size_t>(bra.pp_off + ib) * SB;
-        const Real ip = rb[0], p = rb[1], Px = rb[2], Py = rb[3], Pz = rb[4], Kab = rb[5];
+        const Real p = rb[0], Px = rb[1], Py = rb[2], Pz = rb[3], Wab = rb[4];
         Real G[HAB * NCD];
 #pragma unroll
         for (int x = 0; x < HAB * NCD; ++x) G[x] = Real(0);
@@ -141,11 +142,11 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
         for (int ik = 0; ik < ket.npp; ++ik)
         {
             const Real* __restrict__ rk = tk + static_cast<size_t>(ket.pp_off + ik) * SK;
-            const Real iq = rk[0], q = rk[1];
-            const Real X = Px - rk[2], Y = Py - rk[3], Z = Pz - rk[4];
+            const Real q = rk[0];
+            const Real X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
             const Real rs   = hfg_rsqrt(p + q);
-            const Real rho  = p * q * (rs * rs);
-            const Real pref = Real(kTwoPi25) * (Kab * rk[5]) * (ip * iq) * rs;
+            const Real rho  = (p * q) * (rs * rs);
+            const Real pref = (Wab * rk[4]) * rs;
             const Real T    = rho * (X * X + Y * Y + Z * Z);
             Real F[L + 1];
             boys_eval<L, Real>(T, slice, F);
@@ -180,7 +181,8 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
                                 {
                                     constexpr int e   = decltype(EE)::value;
                                     constexpr int tau = e % lx, nu = (e / lx) % ly, phi = e / (lx * ly);
-                                    const Real term   = rk[eoff + e] * R[hidx(t + tau, u + nu, v + phi, L)];
+                                    const Real rr     = R[hidx(t + tau, u + nu, v + phi, L)];
+                                    const Real term   = (LC + LD == 0) ? rr : rk[eoff + e] * rr;
                                     if constexpr (((tau + nu + phi) & 1) != 0)
                                         s -= term;
                                     else
@@ -206,12 +208,21 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
                         {
                             constexpr int e = decltype(EE)::value;
                             constexpr int t = e % lx, u = (e / lx) % ly, v = e / (lx * ly);
-                            s += rb[eoff + e] * G[hidx(t, u, v, LAB) * NCD + kl];
+                            const Real gg = G[hidx(t, u, v, LAB) * NCD + kl];
+                            s += (LA + LB == 0) ? gg : rb[eoff + e] * gg;
                         });
                     acc[ij * NCD + kl] += s;
                 }
             });
     }
+}
+
+template <typename Real> __device__ __forceinline__ Real ao_threshold(const FockView& v)
+{
+    if constexpr (sizeof(Real) == 4)
+        return v.ao_thr_f;
+    else
+        return v.ao_thr;
 }
 
 template <typename Real> __device__ __forceinline__ Real ldD(const void* p, long long i)
@@ -228,8 +239,8 @@ __device__ __forceinline__ void digest_quartet(const PairRec& bra, const PairRec
     constexpr int NAB = NA * NB, NCD = NC * ND;
     const long long off = v.mat_off[bra.mol];
     const int n         = v.mat_ld[bra.mol];
-    const Real s = Real((bra.same ? 0.5 : 1.0) * (ket.same ? 0.5 : 1.0) * (same_pair ? 0.5 : 1.0));
-    const Real thr = Real(v.ao_thr);
+    const Real s   = (bra.same ? Real(0.5) : Real(1)) * (ket.same ? Real(0.5) : Real(1)) * (same_pair ? Real(0.5) : Real(1));
+    const Real thr = ao_threshold<Real>(v);
     const int a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
     auto at = [&](int r, int c) -> long long { return off + r + static_cast<long long>(c) * n; };
 

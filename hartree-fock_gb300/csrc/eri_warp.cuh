@@ -153,16 +153,16 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
         for (int ib = 0; ib < bra.npp; ++ib)
         {
             const Real* __restrict__ rb = tb + static_cast<size_t>(bra.pp_off + ib) * SB;
-            const Real ip = rb[0], p = rb[1], Px = rb[2], Py = rb[3], Pz = rb[4], Kab = rb[5];
+            const Real p = rb[0], Px = rb[1], Py = rb[2], Pz = rb[3], Wab = rb[4];
             for (int e = lane; e < W::kG; e += 32) Gs[e] = Real(0);
             for (int ik = 0; ik < ket.npp; ++ik)
             {
                 const Real* __restrict__ rk = tk + static_cast<size_t>(ket.pp_off + ik) * SK;
-                const Real iq = rk[0], qq = rk[1];
-                const Real X = Px - rk[2], Y = Py - rk[3], Z = Pz - rk[4];
+                const Real qq = rk[0];
+                const Real X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
                 const Real rs   = hfg_rsqrt(p + qq);
-                const Real rho  = p * qq * (rs * rs);
-                const Real pref = Real(kTwoPi25) * (Kab * rk[5]) * (ip * iq) * rs;
+                const Real rho  = (p * qq) * (rs * rs);
+                const Real pref = (Wab * rk[4]) * rs;
                 const Real T    = rho * (X * X + Y * Y + Z * Z);
                 Real F[L + 1];
                 boys_eval<L, Real>(T, slice, F);
@@ -262,7 +262,8 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
             continue;
         }
         // Angular normalisation, AO-level skip and degeneracy factor, then into shared memory.
-        const Real sdeg = Real((bra.same ? 0.5 : 1.0) * (ket.same ? 0.5 : 1.0) * (qt.bra == qt.ket ? 0.5 : 1.0));
+        const Real sdeg = (bra.same ? Real(0.5) : Real(1)) * (ket.same ? Real(0.5) : Real(1)) * (qt.bra == qt.ket ? Real(0.5) : Real(1));
+        const Real athr = ao_threshold<Real>(v);
 #pragma unroll
         for (int m = 0; m < W::kAcc; ++m)
         {
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
                 const int i = ij / NB, j = ij % NB, k = kl / ND, l = kl % ND;
                 const Real an = Real(ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k) * ang_norm(LD, l));
                 const Real eri = acc[m] * an;
-                Es[e]          = (fabs(eri) < Real(v.ao_thr)) ? Real(0) : sdeg * eri;
+                Es[e]          = (fabs(eri) < athr) ? Real(0) : sdeg * eri;
             }
         }
         __syncwarp();

@@ -98,8 +98,9 @@ __host__ __device__ constexpr int e3_offset(int l1, int l2, int ij)
 }
 __host__ __device__ constexpr int e3_total(int l1, int l2) { return e3_offset(l1, l2, ncart(l1) * ncart(l2)); }
 
-// Per-primitive-pair record: [0] 1/p, [1] p, [2..4] P, [5] Kw (= exp(-ab/p |A-B|^2) * c_a c_b * radial
-// normalisation of both primitives), then e3_total(l1,l2) Hermite coefficients; padded to even.
+// Per-primitive-pair record: [0] p, [1..3] P, [4] W = sqrt(2 pi^{5/2}) / p * exp(-ab/p |A-B|^2) * c_a c_b *
+// radial normalisation of both primitives (so that W_ab W_cd / sqrt(p+q) is the whole primitive
+// prefactor of an ERI), [5] 1/p, then e3_total(l1,l2) Hermite coefficients; padded to even.
 constexpr int kPairHeader = 6;
 __host__ __device__ constexpr int pp_stride(int l1, int l2)
 {
