@@ -22,15 +22,24 @@ constexpr int P2 = QC - P1 * (P1 + 1) / 2;
 constexpr int LA = pair_class_l1(P1), LB = pair_class_l2(P1), LC = pair_class_l1(P2), LD = pair_class_l2(P2);
 constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
 constexpr int L   = LA + LB + LC + LD;
-// Thread-per-quartet when the quartet's register arrays (integrals, G, R) stay small.
-constexpr bool kWarp = (NAB * NCD + nherm(LA + LB) * NCD + nherm(L)) > 128;
+// Kernel form per class and precision, from the ptxas footprint of the thread-per-quartet form
+// (sm_103a, -O3): thread-per-quartet where its stack frame stays at or below ~1.2 KB, the
+// warp-cooperative form for the larger d classes.
+//   FP64 warp: (dp|pp) (dp|ds) (dp|dp) (dd|ps) (dd|pp) (dd|ds) (dd|dp) (dd|dd)   = classes 12-14, 16-20
+//   FP32 warp: (dp|dp) (dd|pp) (dd|ds) (dd|dp) (dd|dd)                           = classes 14, 17-20
+constexpr bool warp_form(bool fp32)
+{
+    return fp32 ? (QC == 14 || QC >= 17) : (QC == 12 || QC == 13 || QC == 14 || QC >= 16);
+}
+constexpr bool kWarp = warp_form(false);
 
 template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
 {
+    constexpr bool kWarpForm = warp_form(sizeof(Real) == 4);
     if (c.count_host == 0)
         return cudaSuccess;
     const size_t slice_bytes = sizeof(Real) * BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow;
-    if constexpr (kWarp)
+    if constexpr (kWarpForm)
     {
         using W             = WarpLayout<LA, LB, LC, LD, Real>;
         const size_t smem   = slice_bytes + sizeof(Real) * W::kPerWarp * kWarpKernelWarps;
