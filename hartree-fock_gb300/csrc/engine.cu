@@ -138,6 +138,7 @@ struct hfg_engine
     hfg::DevBuf<int> d_cls_ids[hfg::kNumPairClasses];
     hfg::DevBuf<double> d_cls_Q[hfg::kNumPairClasses];
     hfg::DevBuf<int4> d_cls_seg[hfg::kNumPairClasses];
+    hfg::DevBuf<int2> d_cls_sh[hfg::kNumPairClasses]; // (sh1, sh2) of each sorted position
     hfg::DevBuf<int2> d_cls_molseg[hfg::kNumPairClasses];
     hfg::DevBuf<unsigned> d_bra_cnt[hfg::kNumQuartetClasses];            // per bra pair: survivors (fp64, fp32)
     hfg::DevBuf<unsigned long long> d_bra_off[hfg::kNumQuartetClasses];  // per bra pair: list offsets
@@ -205,6 +206,7 @@ struct BuildArgs
     int n1;
     const int* ids2;
     const double* Q2;
+    const int2* sh2;     // (sh1, sh2) per ket position
     const int4* seg2;    // ket class segments (equal primitive-pair count, Q descending inside)
     const int2* molseg2; // per molecule: ket segment range
     bool same_class;
@@ -245,9 +247,15 @@ __global__ void build_lists_kernel(BuildArgs a)
     const int2 ms    = a.molseg2[pi.mol];
     const long long so = a.smax_off[pi.mol];
     const int ns = a.nsh[pi.mol];
+    // The shell-max matrices are symmetric: index them so that the ket shell (which varies across the
+    // lanes) is the contiguous one.
     auto M = [&](const double* m, int x, int y) { return m[so + x + (long long)y * ns]; };
     const int sa = pi.sh1, sb = pi.sh2;
     const double dab = 2.0 * M(a.Mt, sa, sb);
+    const double* Ma_a = a.Ma + so + (long long)sa * ns;
+    const double* Ma_b = a.Ma + so + (long long)sb * ns;
+    const double* Mb_a = a.Mb ? a.Mb + so + (long long)sa * ns : nullptr;
+    const double* Mb_b = a.Mb ? a.Mb + so + (long long)sb * ns : nullptr;
     unsigned c64 = 0, c32 = 0;
     unsigned long long p64 = 0, p32 = 0;
     const unsigned long long o64 = a.pass ? a.bra_off[2 * i] : 0ull;
@@ -277,12 +285,12 @@ __global__ void build_lists_kernel(BuildArgs a)
             if (j < jend)
             {
                 pid_j = a.ids2[j];
-                const PairRec pj = a.pairs[pid_j];
-                const int sc = pj.sh1, sd = pj.sh2;
+                const int2 scd = a.sh2[j];
+                const int sc = scd.x, sd = scd.y;
                 double md = fmax(fmax(dab, 2.0 * M(a.Mt, sc, sd)),
-                                 fmax(fmax(M(a.Ma, sa, sc), M(a.Ma, sa, sd)), fmax(M(a.Ma, sb, sc), M(a.Ma, sb, sd))));
-                if (a.Mb)
-                    md = fmax(md, fmax(fmax(M(a.Mb, sa, sc), M(a.Mb, sa, sd)), fmax(M(a.Mb, sb, sc), M(a.Mb, sb, sd))));
+                                 fmax(fmax(Ma_a[sc], Ma_a[sd]), fmax(Ma_b[sc], Ma_b[sd])));
+                if (Mb_a)
+                    md = fmax(md, fmax(fmax(Mb_a[sc], Mb_a[sd]), fmax(Mb_b[sc], Mb_b[sd])));
                 if (md >= a.dthr)
                 {
                     const bool lowp = a.mixed && (Qi * a.Q2[j] * md < a.cutoff);
@@ -763,6 +771,9 @@ static void sort_classes(hfg_engine* e)
             }
             e->cls_molseg[pc][m] = make_int2(first, static_cast<int>(e->cls_seg[pc].size()));
         }
+        std::vector<int2> sh(ids.size());
+        for (size_t k2 = 0; k2 < ids.size(); ++k2) sh[k2] = make_int2(e->pairs[ids[k2]].sh1, e->pairs[ids[k2]].sh2);
+        e->d_cls_sh[pc].upload(sh, e->stream);
         e->d_cls_ids[pc].upload(ids, e->stream);
         e->d_cls_Q[pc].upload(e->cls_Q[pc], e->stream);
         e->d_cls_seg[pc].upload(e->cls_seg[pc], e->stream);
@@ -897,6 +908,7 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
                 a.n1   = static_cast<int>(e->cls_ids[P1].size());
                 a.ids2 = e->d_cls_ids[P2].p;
                 a.Q2   = e->d_cls_Q[P2].p;
+                a.sh2  = e->d_cls_sh[P2].p;
                 a.seg2 = e->d_cls_seg[P2].p;
                 a.molseg2 = e->d_cls_molseg[P2].p;
                 a.same_class = P1 == P2;
