@@ -1,6 +1,7 @@
 // Kernel instantiations and launcher of ONE shell-quartet class.  The build compiles this file once
 // per class with -DHFG_QCLASS=<0..20>, so the 21 classes compile in parallel.
 #include "engine.h"
+#include "eri_grad.cuh"
 
 #ifndef HFG_QCLASS
 #error "compile with -DHFG_QCLASS=<quartet class>"
@@ -88,4 +89,25 @@ cudaError_t HFG_CAT(launch_class_, HFG_QCLASS)(const ClassLaunch& c)
 }
 
 bool HFG_CAT(class_uses_warp_, HFG_QCLASS)() { return kWarp; }
+
+cudaError_t HFG_CAT(launch_grad_, HFG_QCLASS)(const GradLaunch& c)
+{
+    if (c.count == 0)
+        return cudaSuccess;
+    using W           = GradLayout<LA, LB, LC, LD>;
+    const size_t smem = sizeof(double) * (BoysGrid<double>::kPoints * BoysGrid<double>::kRow + W::kPerWarp * kGradWarps);
+    auto kern         = grad_class_kernel<LA, LB, LC, LD>;
+    cudaError_t e     = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kGradWarps, smem);
+    if (e != cudaSuccess)
+        return e;
+    const unsigned long long need = (c.count + kGradWarps - 1) / kGradWarps;
+    const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+    kern<<<static_cast<unsigned>(need < cap ? need : cap), 32 * kGradWarps, smem, c.stream>>>(
+        c.list, c.count, c.view, c.boys_slice, c.tables);
+    return cudaGetLastError();
+}
 } // namespace hfg

@@ -1,10 +1,12 @@
 // Table of the per-class launchers (one translation unit per class, see classes.cu).
 #include "engine.h"
+#include "eri_grad.cuh"
 
 namespace hfg
 {
 #define HFG_DECL(c)                                                                                                    \
     cudaError_t launch_class_##c(const ClassLaunch&);                                                                 \
+    cudaError_t launch_grad_##c(const GradLaunch&);                                                                   \
     bool class_uses_warp_##c();
 HFG_DECL(0) HFG_DECL(1) HFG_DECL(2) HFG_DECL(3) HFG_DECL(4) HFG_DECL(5) HFG_DECL(6) HFG_DECL(7) HFG_DECL(8)
 HFG_DECL(9) HFG_DECL(10) HFG_DECL(11) HFG_DECL(12) HFG_DECL(13) HFG_DECL(14) HFG_DECL(15) HFG_DECL(16)
@@ -22,6 +24,18 @@ static bool (*const kWarp[kNumQuartetClasses])() = {
     class_uses_warp_10, class_uses_warp_11, class_uses_warp_12, class_uses_warp_13, class_uses_warp_14,
     class_uses_warp_15, class_uses_warp_16, class_uses_warp_17, class_uses_warp_18, class_uses_warp_19,
     class_uses_warp_20};
+
+static const decltype(&launch_grad_0) kGrad[kNumQuartetClasses] = {
+    launch_grad_0,  launch_grad_1,  launch_grad_2,  launch_grad_3,  launch_grad_4,  launch_grad_5,  launch_grad_6,
+    launch_grad_7,  launch_grad_8,  launch_grad_9,  launch_grad_10, launch_grad_11, launch_grad_12, launch_grad_13,
+    launch_grad_14, launch_grad_15, launch_grad_16, launch_grad_17, launch_grad_18, launch_grad_19, launch_grad_20};
+
+cudaError_t launch_grad(int qclass, const GradLaunch& L)
+{
+    if (qclass < 0 || qclass >= kNumQuartetClasses)
+        return cudaErrorInvalidValue;
+    return kGrad[qclass](L);
+}
 
 cudaError_t launch_class(int qclass, const ClassLaunch& L)
 {

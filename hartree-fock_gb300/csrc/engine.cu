@@ -13,6 +13,7 @@
 //   lists       per quartet class and precision, the surviving quartets (bra pair, ket pair)
 //   matrices    per molecule n x n column-major blocks, concatenated (dD, X, Y, J, K)
 #include "engine.h"
+#include "eri_grad.cuh"
 #include "hfgpu.h"
 
 #include <algorithm>
@@ -124,8 +125,15 @@ struct hfg_engine
     hfg::DevBuf<int> d_nsh;            // per molecule shell count
     hfg::DevBuf<int> d_shnao;          // per pair: Cartesian counts of sh1, sh2
     hfg::DevBuf<hfg::WarpTables> d_tables;
-    hfg::DevBuf<double> d_boys64[hfg::kMaxLt + 1];
-    hfg::DevBuf<float> d_boys32[hfg::kMaxLt + 1];
+    hfg::DevBuf<double> d_boys64[hfg::kMaxLt + 2];
+    hfg::DevBuf<float> d_boys32[hfg::kMaxLt + 2];
+    hfg::DevBuf<double> d_gtab[hfg::kNumPairClasses]; // gradient records (built on first use)
+    bool have_gtab = false;
+    hfg::DevBuf<int> d_shell_atom;
+    hfg::DevBuf<double> d_grad;
+    // Final state of the last hfg_scf_run (for hfg_gradient's backward call).
+    std::vector<double> scf_Da, scf_Db, scf_W;
+    bool scf_valid = false, scf_uhf = false;
 
     // Schwartz bounds per pair, and per pair class sorted lists.
     std::vector<double> Qpair;
@@ -137,6 +145,7 @@ struct hfg_engine
     std::vector<int2> cls_molseg[hfg::kNumPairClasses]; // per molecule: [first, end) segment
     hfg::DevBuf<int> d_cls_ids[hfg::kNumPairClasses];
     hfg::DevBuf<double> d_cls_Q[hfg::kNumPairClasses];
+    hfg::DevBuf<float> d_cls_Qf[hfg::kNumPairClasses]; // FP32 copy for the precision split
     hfg::DevBuf<int4> d_cls_seg[hfg::kNumPairClasses];
     hfg::DevBuf<int2> d_cls_sh[hfg::kNumPairClasses]; // (sh1, sh2) of each sorted position
     hfg::DevBuf<int2> d_cls_molseg[hfg::kNumPairClasses];
@@ -158,6 +167,8 @@ struct hfg_engine
     hfg::DevBuf<double> d_acc[3];  // X, Ya, Yb
     hfg::DevBuf<double> d_out[3];  // J, Ka, Kb
     hfg::DevBuf<double> d_smax[3]; // shell-pair maxima of |dD|
+    hfg::DevBuf<float> d_smaxf[3]; // FP32 copies (precision split only)
+    hfg::DevBuf<double> d_smax2;   // 2 * shell maxima of |dD_tot|
     hfg::DevBuf<double> d_store;
     hfg::DevBuf<hfg::Quartet> d_tmp_list;
     hfg::DevBuf<unsigned long long> d_tmp_count;
@@ -179,11 +190,14 @@ __global__ void to_float_kernel(const double* __restrict__ a, float* __restrict_
         b[i] = static_cast<float>(a[i]);
 }
 
-// Shell-pair maxima of |dD| (SCF.cpp:544-575) for every molecule block.
+// Shell-pair maxima of |dD| (SCF.cpp:544-575) for every molecule block, with exact integer operations
+// on the bit patterns (|x| clears the sign bit; non-negative doubles order like their bits).  M2, when
+// given, receives 2*M (exact), M32 an FP32 copy.
 __global__ void shell_max_kernel(const double* __restrict__ dD, const PairRec* __restrict__ pairs, int npairs,
                                  const long long* __restrict__ mat_off, const int* __restrict__ mat_ld,
                                  const long long* __restrict__ smax_off, const int* __restrict__ nsh,
-                                 const int* __restrict__ sh_nao, double* __restrict__ M)
+                                 const int* __restrict__ sh_nao, double* __restrict__ M, double* __restrict__ M2,
+                                 float* __restrict__ M32)
 {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x)
     {
@@ -191,11 +205,26 @@ __global__ void shell_max_kernel(const double* __restrict__ dD, const PairRec* _
         const long long off = mat_off[pr.mol];
         const int n = mat_ld[pr.mol], ns = nsh[pr.mol];
         const int n1 = sh_nao[k * 2], n2 = sh_nao[k * 2 + 1];
-        double mx = 0.0;
+        long long mx = 0;
         for (int j = 0; j < n2; ++j)
-            for (int i = 0; i < n1; ++i) mx = fmax(mx, fabs(dD[off + (pr.ao1 + i) + (long long)(pr.ao2 + j) * n]));
-        M[smax_off[pr.mol] + pr.sh1 + (long long)pr.sh2 * ns] = mx;
-        M[smax_off[pr.mol] + pr.sh2 + (long long)pr.sh1 * ns] = mx;
+            for (int i = 0; i < n1; ++i)
+                mx = max(mx, __double_as_longlong(dD[off + (pr.ao1 + i) + (long long)(pr.ao2 + j) * n]) & 0x7fffffffffffffffLL);
+        const double v = __longlong_as_double(mx);
+        const long long e1 = smax_off[pr.mol] + pr.sh1 + (long long)pr.sh2 * ns;
+        const long long e2 = smax_off[pr.mol] + pr.sh2 + (long long)pr.sh1 * ns;
+        M[e1] = v;
+        M[e2] = v;
+        if (M2)
+        {
+            const double v2 = 2.0 * v;
+            M2[e1] = v2;
+            M2[e2] = v2;
+        }
+        if (M32)
+        {
+            M32[e1] = static_cast<float>(v);
+            M32[e2] = static_cast<float>(v);
+        }
     }
 }
 
@@ -212,11 +241,18 @@ struct BuildArgs
     bool same_class;
     const PairRec* pairs;
     const double* Mt;
+    const double* Mt2; // 2 * Mt
     const double* Ma;
     const double* Mb; // null for RHF
+    const float* Qf1;
+    const float* Qf2;
+    const float* Mtf;
+    const float* Maf;
+    const float* Mbf;
     const long long* smax_off;
     const int* nsh;
-    double sthr, dthr, cutoff;
+    double sthr, dthr;
+    float cutoff;
     int mixed;
     int pass;                      // 0: count per bra pair, 1: write at the scanned offsets
     unsigned* bra_cnt;             // [n1][2]
@@ -248,14 +284,16 @@ __global__ void build_lists_kernel(BuildArgs a)
     const long long so = a.smax_off[pi.mol];
     const int ns = a.nsh[pi.mol];
     // The shell-max matrices are symmetric: index them so that the ket shell (which varies across the
-    // lanes) is the contiguous one.
-    auto M = [&](const double* m, int x, int y) { return m[so + x + (long long)y * ns]; };
+    // lanes) is the contiguous one.  Every value here is >= 0, and for non-negative doubles the order of
+    // the IEEE bit patterns is the numeric order, so the maxima and the density test run as exact 64-bit
+    // integer operations (GB300's FP64 pipe is 1/64 of its FP32 rate); the Schwartz product stays FP64.
+    auto bits = [](const double* m, long long i) { return __double_as_longlong(m[i]); };
     const int sa = pi.sh1, sb = pi.sh2;
-    const double dab = 2.0 * M(a.Mt, sa, sb);
-    const double* Ma_a = a.Ma + so + (long long)sa * ns;
-    const double* Ma_b = a.Ma + so + (long long)sb * ns;
-    const double* Mb_a = a.Mb ? a.Mb + so + (long long)sa * ns : nullptr;
-    const double* Mb_b = a.Mb ? a.Mb + so + (long long)sb * ns : nullptr;
+    const long long dab = bits(a.Mt2, so + sa + (long long)sb * ns);
+    const long long dthr = __double_as_longlong(a.dthr);
+    const long long ra = so + (long long)sa * ns, rb2 = so + (long long)sb * ns;
+    const float Qfi = a.Qf1[i];
+    const float dabf = 2.0f * a.Mtf[so + sa + (long long)sb * ns];
     unsigned c64 = 0, c32 = 0;
     unsigned long long p64 = 0, p32 = 0;
     const unsigned long long o64 = a.pass ? a.bra_off[2 * i] : 0ull;
@@ -287,13 +325,22 @@ __global__ void build_lists_kernel(BuildArgs a)
                 pid_j = a.ids2[j];
                 const int2 scd = a.sh2[j];
                 const int sc = scd.x, sd = scd.y;
-                double md = fmax(fmax(dab, 2.0 * M(a.Mt, sc, sd)),
-                                 fmax(fmax(Ma_a[sc], Ma_a[sd]), fmax(Ma_b[sc], Ma_b[sd])));
-                if (Mb_a)
-                    md = fmax(md, fmax(fmax(Mb_a[sc], Mb_a[sd]), fmax(Mb_b[sc], Mb_b[sd])));
-                if (md >= a.dthr)
+                long long md = max(dab, bits(a.Mt2, so + sc + (long long)sd * ns));
+                md = max(md, max(max(bits(a.Ma, ra + sc), bits(a.Ma, ra + sd)), max(bits(a.Ma, rb2 + sc), bits(a.Ma, rb2 + sd))));
+                if (a.Mb)
+                    md = max(md, max(max(bits(a.Mb, ra + sc), bits(a.Mb, ra + sd)), max(bits(a.Mb, rb2 + sc), bits(a.Mb, rb2 + sd))));
+                if (md >= dthr)
                 {
-                    const bool lowp = a.mixed && (Qi * a.Q2[j] * md < a.cutoff);
+                    bool lowp = false;
+                    if (a.mixed)
+                    {
+                        // The FP32/FP64 split is this engine's own heuristic: evaluate it in FP32.
+                        float mf = fmaxf(dabf, 2.0f * a.Mtf[so + sc + (long long)sd * ns]);
+                        mf = fmaxf(mf, fmaxf(fmaxf(a.Maf[ra + sc], a.Maf[ra + sd]), fmaxf(a.Maf[rb2 + sc], a.Maf[rb2 + sd])));
+                        if (a.Mbf)
+                            mf = fmaxf(mf, fmaxf(fmaxf(a.Mbf[ra + sc], a.Mbf[ra + sd]), fmaxf(a.Mbf[rb2 + sc], a.Mbf[rb2 + sd])));
+                        lowp = Qfi * a.Qf2[j] * mf < a.cutoff;
+                    }
                     s32 = lowp;
                     s64 = !lowp;
                 }
@@ -662,7 +709,7 @@ static void pack_molecules(hfg_engine* e)
     build_warp_tables(*tables);
     e->d_tables.alloc(1);
     HFG_CUDA(cudaMemcpyAsync(e->d_tables.p, tables.get(), sizeof(WarpTables), cudaMemcpyHostToDevice, e->stream));
-    for (int L = 0; L <= kMaxLt; ++L)
+    for (int L = 0; L <= kMaxLt + 1; ++L)
     {
         e->d_boys64[L].upload(boys_slice_host<double>(L), e->stream);
         e->d_boys32[L].upload(boys_slice_host<float>(L), e->stream);
@@ -776,6 +823,10 @@ static void sort_classes(hfg_engine* e)
         e->d_cls_sh[pc].upload(sh, e->stream);
         e->d_cls_ids[pc].upload(ids, e->stream);
         e->d_cls_Q[pc].upload(e->cls_Q[pc], e->stream);
+        {
+            std::vector<float> qf(e->cls_Q[pc].begin(), e->cls_Q[pc].end());
+            e->d_cls_Qf[pc].upload(qf, e->stream);
+        }
         e->d_cls_seg[pc].upload(e->cls_seg[pc], e->stream);
         e->d_cls_molseg[pc].upload(e->cls_molseg[pc], e->stream);
     }
@@ -833,6 +884,101 @@ static void size_lists(hfg_engine* e, double sthr, bool mixed)
     e->cap_mixed = mixed;
 }
 
+// Screening and the survival lists of every quartet class from the densities already in d_dD[0..2]
+// (the shell-pair maxima, then count pass, scan and write pass per class).  Returns the launches.
+static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double dthr, double cutoff)
+{
+    cudaStream_t s  = e->stream;
+    const int nspin = uhf ? 3 : 2;
+    // Shell-pair maxima (and their FP32 copies for the precision split).
+    for (int k = 0; k < nspin; ++k)
+    {
+        e->d_smaxf[k].alloc(e->smax_total);
+        if (k == 0)
+            e->d_smax2.alloc(e->smax_total);
+        shell_max_kernel<<<grid_for(e->pairs.size(), 128, e->num_sms), 128, 0, s>>>(
+            e->d_dD[k].p, e->d_pairs.p, static_cast<int>(e->pairs.size()), e->d_mat_off.p, e->d_mat_ld.p, e->d_smax_off.p,
+            e->d_nsh.p, e->d_shnao.p, e->d_smax[k].p, k == 0 ? e->d_smax2.p : nullptr, mixed ? e->d_smaxf[k].p : nullptr);
+        HFG_CUDA(cudaGetLastError());
+    }
+
+    // Lists: count pass, scan, write pass, per quartet class.
+    const int ncnt = kNumQuartetClasses * 2;
+    e->d_counts.alloc(2 * ncnt + 1);
+    HFG_CUDA(cudaMemsetAsync(e->d_counts.p, 0, sizeof(unsigned long long) * (2 * ncnt + 1), s));
+    int launches = 0;
+    size_t max_blocks = 1;
+    for (int P1 = 0; P1 < kNumPairClasses; ++P1)
+        max_blocks = std::max(max_blocks, (e->cls_ids[P1].size() + kScanBlock - 1) / kScanBlock);
+    e->d_scan_tmp.alloc(2 * max_blocks);
+    for (int pass = 0; pass < 2; ++pass)
+        for (int P1 = 0; P1 < kNumPairClasses; ++P1)
+            for (int P2 = 0; P2 <= P1; ++P2)
+            {
+                const int qc = quartet_class(P1, P2);
+                if (e->cap[qc] == 0 || e->cls_ids[P1].empty() || e->cls_ids[P2].empty())
+                    continue;
+                BuildArgs a {};
+                a.ids1 = e->d_cls_ids[P1].p;
+                a.Q1   = e->d_cls_Q[P1].p;
+                a.n1   = static_cast<int>(e->cls_ids[P1].size());
+                a.ids2 = e->d_cls_ids[P2].p;
+                a.Q2   = e->d_cls_Q[P2].p;
+                a.sh2  = e->d_cls_sh[P2].p;
+                a.seg2 = e->d_cls_seg[P2].p;
+                a.molseg2 = e->d_cls_molseg[P2].p;
+                a.same_class = P1 == P2;
+                a.pairs = e->d_pairs.p;
+                a.Mt = e->d_smax[0].p;
+                a.Mt2 = e->d_smax2.p;
+                a.Ma = e->d_smax[1].p;
+                a.Mb = uhf ? e->d_smax[2].p : nullptr;
+                a.Qf1 = e->d_cls_Qf[P1].p;
+                a.Qf2 = e->d_cls_Qf[P2].p;
+                a.Mtf = mixed ? e->d_smaxf[0].p : nullptr;
+                a.Maf = mixed ? e->d_smaxf[1].p : nullptr;
+                a.Mbf = (mixed && uhf) ? e->d_smaxf[2].p : nullptr;
+                a.smax_off = e->d_smax_off.p;
+                a.nsh = e->d_nsh.p;
+                a.sthr = sthr;
+                a.dthr = dthr;
+                a.cutoff = static_cast<float>(cutoff);
+                a.mixed = mixed ? 1 : 0;
+                a.pass = pass;
+                a.bra_cnt = e->d_bra_cnt[qc].p;
+                a.bra_off = e->d_bra_off[qc].p;
+                a.out64 = e->d_list[qc][0].p;
+                a.out32 = mixed ? e->d_list[qc][1].p : nullptr;
+                a.prim64 = e->d_counts.p + ncnt + 2 * qc;
+                a.prim32 = e->d_counts.p + ncnt + 2 * qc + 1;
+                a.cap = e->cap[qc];
+                const long long threads = static_cast<long long>(a.n1) * 32;
+                build_lists_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, s>>>(a);
+                HFG_CUDA(cudaGetLastError());
+                ++launches;
+                if (pass == 0)
+                {
+                    const int nb = (a.n1 + kScanBlock - 1) / kScanBlock;
+                    scan_block_kernel<<<nb, kScanBlock, 0, s>>>(e->d_bra_cnt[qc].p, e->d_bra_off[qc].p, a.n1,
+                                                                e->d_scan_tmp.p);
+                    scan_tops_kernel<<<1, 32, 0, s>>>(e->d_scan_tmp.p, nb, e->d_counts.p + 2 * qc);
+                    scan_add_kernel<<<nb, kScanBlock, 0, s>>>(e->d_bra_off[qc].p, a.n1, e->d_scan_tmp.p);
+                    HFG_CUDA(cudaGetLastError());
+                    launches += 3;
+                }
+            }
+    e->h_counts.assign(2 * ncnt + 1, 0);
+    HFG_CUDA(cudaMemcpyAsync(e->h_counts.data(), e->d_counts.p, sizeof(unsigned long long) * (2 * ncnt + 1),
+                             cudaMemcpyDeviceToHost, s));
+    HFG_CUDA(cudaEventRecord(e->ev[2], s));
+    HFG_CUDA(cudaStreamSynchronize(s));
+    for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+        if (e->h_counts[2 * qc] > e->cap[qc] || e->h_counts[2 * qc + 1] > e->cap[qc])
+            throw HfgError(HFG_ERR_OVERFLOW, "fock: quartet list overflow");
+
+    return launches + nspin;
+}
+
 static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats* st)
 {
     if (!(r.schwartz_threshold >= 0.0) || !(r.density_threshold >= 0.0) || !std::isfinite(r.schwartz_threshold) ||
@@ -877,82 +1023,8 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
     }
     HFG_CUDA(cudaEventRecord(e->ev[1], s));
 
-    // Shell-pair maxima.
-    for (int k = 0; k < nspin; ++k)
-    {
-        shell_max_kernel<<<grid_for(e->pairs.size(), 128, e->num_sms), 128, 0, s>>>(
-            e->d_dD[k].p, e->d_pairs.p, static_cast<int>(e->pairs.size()), e->d_mat_off.p, e->d_mat_ld.p, e->d_smax_off.p,
-            e->d_nsh.p, e->d_shnao.p, e->d_smax[k].p);
-        HFG_CUDA(cudaGetLastError());
-    }
-
-    // Lists: count pass, scan, write pass, per quartet class.
+    int launches = nspin * (mixed ? 2 : 1) + build_lists(e, uhf, mixed, r.schwartz_threshold, r.density_threshold, r.fp32_cutoff);
     const int ncnt = kNumQuartetClasses * 2;
-    e->d_counts.alloc(2 * ncnt + 1);
-    HFG_CUDA(cudaMemsetAsync(e->d_counts.p, 0, sizeof(unsigned long long) * (2 * ncnt + 1), s));
-    int launches = nspin * (mixed ? 2 : 1) + nspin;
-    size_t max_blocks = 1;
-    for (int P1 = 0; P1 < kNumPairClasses; ++P1)
-        max_blocks = std::max(max_blocks, (e->cls_ids[P1].size() + kScanBlock - 1) / kScanBlock);
-    e->d_scan_tmp.alloc(2 * max_blocks);
-    for (int pass = 0; pass < 2; ++pass)
-        for (int P1 = 0; P1 < kNumPairClasses; ++P1)
-            for (int P2 = 0; P2 <= P1; ++P2)
-            {
-                const int qc = quartet_class(P1, P2);
-                if (e->cap[qc] == 0 || e->cls_ids[P1].empty() || e->cls_ids[P2].empty())
-                    continue;
-                BuildArgs a {};
-                a.ids1 = e->d_cls_ids[P1].p;
-                a.Q1   = e->d_cls_Q[P1].p;
-                a.n1   = static_cast<int>(e->cls_ids[P1].size());
-                a.ids2 = e->d_cls_ids[P2].p;
-                a.Q2   = e->d_cls_Q[P2].p;
-                a.sh2  = e->d_cls_sh[P2].p;
-                a.seg2 = e->d_cls_seg[P2].p;
-                a.molseg2 = e->d_cls_molseg[P2].p;
-                a.same_class = P1 == P2;
-                a.pairs = e->d_pairs.p;
-                a.Mt = e->d_smax[0].p;
-                a.Ma = e->d_smax[1].p;
-                a.Mb = uhf ? e->d_smax[2].p : nullptr;
-                a.smax_off = e->d_smax_off.p;
-                a.nsh = e->d_nsh.p;
-                a.sthr = r.schwartz_threshold;
-                a.dthr = r.density_threshold;
-                a.cutoff = r.fp32_cutoff;
-                a.mixed = mixed ? 1 : 0;
-                a.pass = pass;
-                a.bra_cnt = e->d_bra_cnt[qc].p;
-                a.bra_off = e->d_bra_off[qc].p;
-                a.out64 = e->d_list[qc][0].p;
-                a.out32 = mixed ? e->d_list[qc][1].p : nullptr;
-                a.prim64 = e->d_counts.p + ncnt + 2 * qc;
-                a.prim32 = e->d_counts.p + ncnt + 2 * qc + 1;
-                a.cap = e->cap[qc];
-                const long long threads = static_cast<long long>(a.n1) * 32;
-                build_lists_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, s>>>(a);
-                HFG_CUDA(cudaGetLastError());
-                ++launches;
-                if (pass == 0)
-                {
-                    const int nb = (a.n1 + kScanBlock - 1) / kScanBlock;
-                    scan_block_kernel<<<nb, kScanBlock, 0, s>>>(e->d_bra_cnt[qc].p, e->d_bra_off[qc].p, a.n1,
-                                                                e->d_scan_tmp.p);
-                    scan_tops_kernel<<<1, 32, 0, s>>>(e->d_scan_tmp.p, nb, e->d_counts.p + 2 * qc);
-                    scan_add_kernel<<<nb, kScanBlock, 0, s>>>(e->d_bra_off[qc].p, a.n1, e->d_scan_tmp.p);
-                    HFG_CUDA(cudaGetLastError());
-                    launches += 3;
-                }
-            }
-    e->h_counts.assign(2 * ncnt + 1, 0);
-    HFG_CUDA(cudaMemcpyAsync(e->h_counts.data(), e->d_counts.p, sizeof(unsigned long long) * (2 * ncnt + 1),
-                             cudaMemcpyDeviceToHost, s));
-    HFG_CUDA(cudaEventRecord(e->ev[2], s));
-    HFG_CUDA(cudaStreamSynchronize(s));
-    for (int qc = 0; qc < kNumQuartetClasses; ++qc)
-        if (e->h_counts[2 * qc] > e->cap[qc] || e->h_counts[2 * qc + 1] > e->cap[qc])
-            throw HfgError(HFG_ERR_OVERFLOW, "fock: quartet list overflow");
 
     // Class kernels: FP64 lists, then FP32 lists.
     for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
@@ -1044,6 +1116,124 @@ void engine_set_error(hfg_engine* e, const std::string& msg)
 {
     if (e)
         e->last_error = msg;
+}
+
+// Gradient records per primitive pair (same order as the forward tables): a, b and the 1-D Hermite
+// tables E[i][j][t] up to (l1+1, l2+1) of the three axes.
+static void build_grad_tables(hfg_engine* e)
+{
+    if (e->have_gtab)
+        return;
+    std::vector<std::vector<double>> tab(kNumPairClasses);
+    for (size_t k = 0; k < e->pairs.size(); ++k)
+    {
+        const PairRec& pr = e->pairs[k];
+        const int pc = e->pair_class_of[k];
+        const HostBasis& b = e->basis[pr.mol];
+        const int l1 = b.l[pr.sh1], l2 = b.l[pr.sh2];
+        const int stride = g_stride(l1, l2), n1 = g1d_size(l1, l2);
+        if (tab[pc].size() < static_cast<size_t>(pr.pp_off + pr.npp) * stride)
+            tab[pc].resize(static_cast<size_t>(pr.pp_off + pr.npp) * stride, 0.0);
+        const double* A = &b.centers[3 * pr.sh1];
+        const double* B = &b.centers[3 * pr.sh2];
+        int idx = 0;
+        for (int pa = 0; pa < b.nprim[pr.sh1]; ++pa)
+            for (int pb = 0; pb < b.nprim[pr.sh2]; ++pb, ++idx)
+            {
+                const double aa = b.alpha[b.prim_off[pr.sh1] + pa], ab = b.alpha[b.prim_off[pr.sh2] + pb];
+                const double p = aa + ab, ip = 1.0 / p, h = 0.5 * ip;
+                double* rec = &tab[pc][static_cast<size_t>(pr.pp_off + idx) * stride];
+                rec[0] = aa;
+                rec[1] = ab;
+                for (int ax = 0; ax < 3; ++ax)
+                {
+                    const double P = (aa * A[ax] + ab * B[ax]) * ip, PA = P - A[ax], PB = P - B[ax];
+                    double* E = rec + 2 + ax * n1;
+                    auto at = [&](int i, int j, int t) -> double& { return E[(i * (l2 + 2) + j) * (l1 + l2 + 3) + t]; };
+                    at(0, 0, 0) = 1.0;
+                    for (int i = 0; i <= l1 + 1; ++i)
+                        for (int j = 0; j <= l2 + 1; ++j)
+                        {
+                            if (i == 0 && j == 0)
+                                continue;
+                            const bool up_i = i > 0;
+                            const int pi = up_i ? i - 1 : i, pj = up_i ? j : j - 1;
+                            const double X = up_i ? PA : PB;
+                            for (int t = 0; t <= i + j; ++t)
+                            {
+                                double v = 0.0;
+                                if (t <= pi + pj)
+                                    v += X * at(pi, pj, t);
+                                if (t >= 1)
+                                    v += h * at(pi, pj, t - 1);
+                                if (t + 1 <= pi + pj)
+                                    v += (t + 1) * at(pi, pj, t + 1);
+                                at(i, j, t) = v;
+                            }
+                        }
+                }
+            }
+    }
+    for (int pc = 0; pc < kNumPairClasses; ++pc) e->d_gtab[pc].upload(tab[pc], e->stream);
+    HFG_CUDA(cudaStreamSynchronize(e->stream));
+    e->have_gtab = true;
+}
+
+// Two-electron part of the nuclear gradient on the device (eri_grad.cuh) for the densities in
+// d_dD[0..2] (total, alpha, beta); adds into grad[3*natom] (host).  Returns the device milliseconds.
+static double gradient_two_electron(hfg_engine* e, const std::vector<int>& shell_atom, int natom, bool uhf,
+                                    double sthr, double dthr, double* grad)
+{
+    cudaStream_t s = e->stream;
+    build_grad_tables(e);
+    e->d_shell_atom.upload(shell_atom, s);
+    e->d_grad.alloc(static_cast<size_t>(3) * natom);
+    HFG_CUDA(cudaMemsetAsync(e->d_grad.p, 0, sizeof(double) * 3 * natom, s));
+    size_lists(e, sthr, false);
+    build_lists(e, uhf, false, sthr, dthr, 0.0);
+    GradView v {};
+    v.pairs = e->d_pairs.p;
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        v.pptab[pc] = e->d_pptab64[pc].p;
+        v.gtab[pc]  = e->d_gtab[pc].p;
+    }
+    v.Dt = e->d_dD[0].p;
+    v.Da = e->d_dD[1].p;
+    v.Db = uhf ? e->d_dD[2].p : e->d_dD[1].p;
+    v.n = e->mols[0].nao;
+    v.shell_atom = e->d_shell_atom.p;
+    v.grad = e->d_grad.p;
+    HFG_CUDA(cudaEventRecord(e->ev[6], s));
+    for (int qc = kNumQuartetClasses - 1; qc >= 0; --qc)
+    {
+        const unsigned long long n = e->h_counts[2 * qc];
+        if (n == 0)
+            continue;
+        const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+        const int P2 = qc - P1 * (P1 + 1) / 2;
+        const int L  = pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2);
+        GradLaunch g {e->d_list[qc][0].p, n, v, e->d_boys64[L + 1].p, e->d_tables.p, s, e->num_sms};
+        HFG_CUDA(launch_grad(qc, g));
+    }
+    HFG_CUDA(cudaEventRecord(e->ev[7], s));
+    std::vector<double> g(static_cast<size_t>(3) * natom);
+    HFG_CUDA(cudaMemcpyAsync(g.data(), e->d_grad.p, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s));
+    HFG_CUDA(cudaStreamSynchronize(s));
+    for (size_t k = 0; k < g.size(); ++k) grad[k] += g[k];
+    float ms = 0.f;
+    HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
+    return ms;
+}
+
+void engine_store_scf_state(hfg_engine* e, const double* Da, const double* Db, const double* W, bool uhf)
+{
+    const size_t N2 = static_cast<size_t>(e->mols[0].nao) * e->mols[0].nao;
+    e->scf_Da.assign(Da, Da + N2);
+    e->scf_Db.assign(Db, Db + N2);
+    e->scf_W.assign(W, W + N2);
+    e->scf_uhf   = uhf;
+    e->scf_valid = true;
 }
 
 // Work model (per primitive quartet of class (la lb|lc ld), L = sum): the R recursion (one FMA per
@@ -1292,6 +1482,67 @@ int hfg_survivors(hfg_engine* e, int* quartets, long long cap, long long* count)
         if (quartets)
             for (long long k = 0; k < std::min<long long>(cap, *count); ++k)
                 for (int j = 0; j < 4; ++j) quartets[4 * k + j] = all[k][j + 1];
+    });
+}
+
+int hfg_gradient(hfg_engine* e, const hfg_gradient_request* r, double* grad, double* ms_two_electron)
+{
+    if (!e || !r || !grad || r->natom <= 0 || !r->Z || !r->xyz)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        if (e->nmol != 1)
+            throw HfgError(HFG_ERR_INVALID, "hfg_gradient: the engine must hold exactly one molecule");
+        HFG_CUDA(cudaSetDevice(e->device));
+        const int n = e->mols[0].nao;
+        const size_t N2 = static_cast<size_t>(n) * n;
+        const bool use_last = r->D_alpha == nullptr;
+        if (use_last && !e->scf_valid)
+            throw HfgError(HFG_ERR_INVALID, "hfg_gradient: no densities given and no SCF run on this engine");
+        const bool uhf = use_last ? e->scf_uhf : (r->unrestricted != 0);
+        const double* Da = use_last ? e->scf_Da.data() : r->D_alpha;
+        const double* Db = use_last ? e->scf_Db.data() : (uhf ? r->D_beta : r->D_alpha);
+        const double* W  = use_last ? e->scf_W.data() : r->W;
+        if (!Db || !W)
+            throw HfgError(HFG_ERR_INVALID, "hfg_gradient: missing D_beta or W");
+        // Shell -> atom from the shell centres.
+        const auto& hb = e->basis[0];
+        std::vector<int> shell_atom(hb.l.size(), -1);
+        for (size_t sh = 0; sh < hb.l.size(); ++sh)
+        {
+            for (int a = 0; a < r->natom; ++a)
+                if (hb.centers[3 * sh] == r->xyz[3 * a] && hb.centers[3 * sh + 1] == r->xyz[3 * a + 1] &&
+                    hb.centers[3 * sh + 2] == r->xyz[3 * a + 2])
+                {
+                    shell_atom[sh] = a;
+                    break;
+                }
+            if (shell_atom[sh] < 0)
+                throw HfgError(HFG_ERR_INVALID, "hfg_gradient: a shell centre matches no nucleus");
+        }
+        std::vector<double> Dt(N2);
+        for (size_t k = 0; k < N2; ++k) Dt[k] = Da[k] + Db[k];
+        for (int k = 0; k < 3; ++k)
+        {
+            e->d_dD[k].alloc(N2);
+            e->d_smax[k].alloc(e->smax_total);
+        }
+        if (!e->have_Q)
+        {
+            hfg::compute_schwartz(e);
+            hfg::sort_classes(e);
+        }
+        HFG_CUDA(cudaMemcpyAsync(e->d_dD[0].p, Dt.data(), sizeof(double) * N2, cudaMemcpyHostToDevice, e->stream));
+        HFG_CUDA(cudaMemcpyAsync(e->d_dD[1].p, Da, sizeof(double) * N2, cudaMemcpyHostToDevice, e->stream));
+        HFG_CUDA(cudaMemcpyAsync(e->d_dD[2].p, Db, sizeof(double) * N2, cudaMemcpyHostToDevice, e->stream));
+        std::fill(grad, grad + 3 * r->natom, 0.0);
+        const double ms = hfg::gradient_two_electron(e, shell_atom, r->natom, true, r->schwartz_threshold,
+                                                     r->density_threshold, grad);
+        if (ms_two_electron)
+            *ms_two_electron = ms;
+        e->last_valid = false; // the lists now hold the gradient's quartets
+        const int rc = hfg_gradient_one_electron(&hb.view, shell_atom.data(), r->natom, r->Z, r->xyz, Dt.data(), W, grad);
+        if (rc != HFG_OK)
+            throw HfgError(rc, "hfg_gradient: one-electron part failed");
     });
 }
 

@@ -30,9 +30,18 @@ using ClassLauncher = cudaError_t (*)(const ClassLaunch&);
 cudaError_t launch_class(int qclass, const ClassLaunch& L);
 bool class_uses_warp_kernel(int qclass);
 
-// Schwartz kernel launch for pair class pc (defined in classes_schwartz.cu).
-cudaError_t launch_schwartz(int pc, const int* pair_ids, int npairs, const FockView& v, const double* boys_slice,
-                            double* Q, cudaStream_t stream, int num_sms);
+struct GradView;
+struct GradLaunch
+{
+    const Quartet* list;
+    unsigned long long count;
+    const GradView& view;
+    const double* boys_slice; // slice for total L + 1
+    const WarpTables* tables;
+    cudaStream_t stream;
+    int num_sms;
+};
+cudaError_t launch_grad(int qclass, const GradLaunch& L);
 
 // Work model: algorithmic FLOPs of one primitive quartet and of one shell quartet's digestion.
 double flops_per_prim_quartet(int qclass);

@@ -1,0 +1,308 @@
+// Adjoint two-electron part of the analytic nuclear gradient (no counterpart in the reference, which has
+// no gradients; the differentiated integrals are those of src/IntegralEngine.cpp:731-992).
+//
+//   dE_2e/dX = 1/2 sum_{ijkl} d(ij|kl)/dX Gamma_ijkl,
+//   Gamma_ijkl = Dt_ij Dt_kl - 1/2 sum_s (Ds_ik Ds_jl + Ds_il Ds_jk)        (s = alpha, beta)
+//
+// summed over unique shell quartets with the degeneracy factor s_q (1/2 per equal pair, as in the
+// Fock build): dE/dX = 4 sum_q s_q sum_{ijkl in q} Gamma_ijkl d(ij|kl)/dX.
+//
+// Centre derivatives in McMurchie-Davidson form: d/dA_x of a primitive pair distribution has Hermite
+// coefficients  DA^{ij}_t = 2a E^{i+1,j}_t - i E^{i-1,j}_t  (x factor; y and z factors unchanged), likewise
+// DB with b and j, DC/DD on the ket.  The kernel never forms derivative integrals: per primitive quartet
+//   G[tuv][kl]  = sum_{tau nu phi} (-1)^{tau+nu+phi} E^{kl}_{tau nu phi} R_{t+tau,..}   (t+u+v <= l_ab + 1)
+//   y[ij][tuv]  = sum_kl Gamma_ijkl G[tuv][kl]          -> g_A += DA . y,  g_B += DB . y
+//   X[ij][tuv'] = sum_{tuv} E^{ij}_{tuv} R_{t+tau,..}   (tau+nu+phi <= l_cd + 1)
+//   h[kl][tuv'] = sum_ij Gamma_ijkl X[ij][tuv']         -> g_C += (-1)^{..} DC . h
+// and g_D = -(g_A + g_B + g_C) (translational invariance).  E/R tables are recomputed here, nothing from
+// the forward build is stored.  One warp per quartet; FP64.
+#pragma once
+
+#include "eri_warp.cuh"
+
+namespace hfg
+{
+// Per-primitive-pair gradient record for pair class (l1, l2): [0] a, [1] b, then for each axis the 1-D
+// Hermite table E[i][j][t], i <= l1+1, j <= l2+1, t <= l1+l2+2 (dense).
+__host__ __device__ constexpr int g1d_size(int l1, int l2) { return (l1 + 2) * (l2 + 2) * (l1 + l2 + 3); }
+__host__ __device__ constexpr int g_stride(int l1, int l2)
+{
+    const int s = 2 + 3 * g1d_size(l1, l2);
+    return s + (s & 1);
+}
+
+struct GradView
+{
+    const PairRec* pairs;
+    const double* pptab[kNumPairClasses]; // forward records (p, P, W, ...)
+    const double* gtab[kNumPairClasses];  // gradient records
+    const double* Dt;
+    const double* Da;
+    const double* Db;
+    int n;                  // nao
+    const int* shell_atom;  // per shell
+    double* grad;           // [natom][3]
+};
+
+#ifdef __CUDACC__
+template <int LA, int LB, int LC, int LD> struct GradLayout
+{
+    static constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    static constexpr int NAB = NA * NB, NCD = NC * ND;
+    static constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD + 1;
+    static constexpr int HAB1 = nherm(LAB + 1), HCD1 = nherm(LCD + 1), HL = nherm(L);
+    static constexpr int kR = 2 * HL, kG = HAB1 * NCD, kX = NAB * HCD1, kGam = NAB * NCD;
+    static constexpr int kPerWarp = ((kR + kG + kX + kGam + 1) / 2) * 2;
+};
+
+constexpr int kGradWarps = 2;
+
+__device__ __forceinline__ double e1(const double* T, int l2, int l12, int i, int j, int t)
+{
+    // T: one axis of a gradient record, dense [i][j][t] with extents (l1+2, l2+2, l12+3)
+    return T[(i * (l2 + 2) + j) * (l12 + 3) + t];
+}
+
+template <int LA, int LB, int LC, int LD>
+__global__ void __launch_bounds__(32 * kGradWarps)
+    grad_class_kernel(const Quartet* __restrict__ list, unsigned long long n, GradView v,
+                      const double* __restrict__ boys_slice, const WarpTables* __restrict__ tabs)
+{
+    using W = GradLayout<LA, LB, LC, LD>;
+    constexpr int NA = W::NA, NB = W::NB, NC = W::NC, ND = W::ND, NAB = W::NAB, NCD = W::NCD;
+    constexpr int LAB = W::LAB, LCD = W::LCD, L = W::L, HAB1 = W::HAB1, HCD1 = W::HCD1, HL = W::HL;
+    constexpr int SB = pp_stride(LA, LB), SK = pp_stride(LC, LD);
+    constexpr int GB = g_stride(LA, LB), GK = g_stride(LC, LD);
+    constexpr int PCB = pair_class(LA, LB), PCK = pair_class(LC, LD);
+    constexpr int S = L + 1;
+    constexpr int G1B = g1d_size(LA, LB), G1K = g1d_size(LC, LD);
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* slice = reinterpret_cast<double*>(smem_raw);
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    if (static_cast<unsigned long long>(blockIdx.x) * kGradWarps >= n)
+        return;
+    stage_boys<double>(boys_slice, slice);
+    double* wbase = slice + BoysGrid<double>::kPoints * BoysGrid<double>::kRow + wib * W::kPerWarp;
+    double* Rbuf0 = wbase;
+    double* Rbuf1 = wbase + HL;
+    double* Gs    = wbase + 2 * HL;
+    double* Xs    = Gs + W::kG;
+    double* Gam   = Xs + W::kX;
+
+    for (unsigned long long q = static_cast<unsigned long long>(blockIdx.x) * kGradWarps + wib; q < n;
+         q += static_cast<unsigned long long>(gridDim.x) * kGradWarps)
+    {
+        const Quartet qt  = list[q];
+        const PairRec bra = v.pairs[qt.bra];
+        const PairRec ket = v.pairs[qt.ket];
+        const int a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
+        const int n = v.n;
+        const double sdeg = 4.0 * (bra.same ? 0.5 : 1.0) * (ket.same ? 0.5 : 1.0) * (qt.bra == qt.ket ? 0.5 : 1.0);
+        // Gamma (with the angular normalisation of the four components and the degeneracy factor).
+        for (int e = lane; e < NAB * NCD; e += 32)
+        {
+            const int ij = e / NCD, kl = e % NCD;
+            const int i = ij / NB, j = ij % NB, k = kl / ND, l = kl % ND;
+            const long long I = a0 + i, J = b0 + j, K = c0 + k, Lx = d0 + l;
+            auto D = [&](const double* M, long long r, long long c) { return M[r + c * n]; };
+            const double g = D(v.Dt, I, J) * D(v.Dt, K, Lx) -
+                             0.5 * (D(v.Da, I, K) * D(v.Da, J, Lx) + D(v.Da, I, Lx) * D(v.Da, J, K) +
+                                    D(v.Db, I, K) * D(v.Db, J, Lx) + D(v.Db, I, Lx) * D(v.Db, J, K));
+            Gam[e] = sdeg * ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k) * ang_norm(LD, l) * g;
+        }
+        __syncwarp();
+        double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+
+        for (int ib = 0; ib < bra.npp; ++ib)
+        {
+            const double* __restrict__ rb = v.pptab[PCB] + static_cast<size_t>(bra.pp_off + ib) * SB;
+            const double* __restrict__ gb = v.gtab[PCB] + static_cast<size_t>(bra.pp_off + ib) * GB;
+            const double p = rb[0], Px = rb[1], Py = rb[2], Pz = rb[3], Wab = rb[4];
+            const double aexp = gb[0], bexp = gb[1];
+            for (int ik = 0; ik < ket.npp; ++ik)
+            {
+                const double* __restrict__ rk = v.pptab[PCK] + static_cast<size_t>(ket.pp_off + ik) * SK;
+                const double* __restrict__ gk = v.gtab[PCK] + static_cast<size_t>(ket.pp_off + ik) * GK;
+                const double qq = rk[0];
+                const double X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
+                const double rs   = hfg_rsqrt(p + qq);
+                const double rho  = (p * qq) * (rs * rs);
+                const double pref = (Wab * rk[4]) * rs;
+                const double T    = rho * (X * X + Y * Y + Z * Z);
+                const double cexp = gk[0];
+                double F[L + 1];
+                boys_eval<L, double>(T, slice, F);
+                double Fs[L + 1];
+                {
+                    const double m2r = -2.0 * rho;
+                    double w         = pref;
+#pragma unroll
+                    for (int k = 0; k <= L; ++k)
+                    {
+                        Fs[k] = w * F[k];
+                        w *= m2r;
+                    }
+                }
+                double* src = Rbuf0;
+                double* dst = Rbuf1;
+                if (lane == 0)
+                    src[0] = Fs[L];
+                __syncwarp();
+#pragma unroll
+                for (int lev = L - 1; lev >= 0; --lev)
+                {
+                    const int cnt = nherm(L - lev);
+                    for (int k = 1 + lane; k < cnt; k += 32)
+                    {
+                        const int4 r  = tabs->rtab[L][k];
+                        const int ax  = r.w & 3, c = r.w >> 2;
+                        const double xa = ax == 0 ? X : (ax == 1 ? Y : Z);
+                        double val    = xa * src[r.y];
+                        if (c > 0)
+                            val += double(c) * src[r.z];
+                        dst[r.x] = val;
+                    }
+                    if (lane == 0)
+                        dst[0] = Fs[lev];
+                    __syncwarp();
+                    double* t = src;
+                    src       = dst;
+                    dst       = t;
+                }
+                const double* R = src;
+                auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
+
+                // G[tuv][kl] over t+u+v <= LAB+1, and X[ij][tuv'] over t+u+v <= LCD+1.
+                for (int e = lane; e < HAB1 * NCD; e += 32)
+                {
+                    const int h = e / NCD, kl = e % NCD;
+                    const int tuv = tabs->htuv[LAB + 1][h];
+                    const int t = tuv & 255, u = (tuv >> 8) & 255, w_ = tuv >> 16;
+                    const int k = kl / ND, l = kl % ND;
+                    const int kx = cart_exp(LC, k, 0), ky = cart_exp(LC, k, 1), kz = cart_exp(LC, k, 2);
+                    const int lx = cart_exp(LD, l, 0), ly = cart_exp(LD, l, 1), lz = cart_exp(LD, l, 2);
+                    const double* Ex = gk + 2;
+                    const double* Ey = Ex + G1K;
+                    const double* Ez = Ey + G1K;
+                    double s = 0.0;
+                    for (int ph = 0; ph <= kz + lz; ++ph)
+                        for (int nu = 0; nu <= ky + ly; ++nu)
+                        {
+                            const double eyz = e1(Ey, LD, LCD, ky, ly, nu) * e1(Ez, LD, LCD, kz, lz, ph);
+                            for (int ta = 0; ta <= kx + lx; ++ta)
+                            {
+                                const double term = eyz * e1(Ex, LD, LCD, kx, lx, ta) * Ridx(t + ta, u + nu, w_ + ph);
+                                s += ((ta + nu + ph) & 1) ? -term : term;
+                            }
+                        }
+                    Gs[e] = s;
+                }
+                for (int e = lane; e < NAB * HCD1; e += 32)
+                {
+                    const int ij = e / HCD1, h = e % HCD1;
+                    const int tuv = tabs->htuv[LCD + 1][h];
+                    const int ta = tuv & 255, nu = (tuv >> 8) & 255, ph = tuv >> 16;
+                    const int i = ij / NB, j = ij % NB;
+                    const int ix = cart_exp(LA, i, 0), iy = cart_exp(LA, i, 1), iz = cart_exp(LA, i, 2);
+                    const int jx = cart_exp(LB, j, 0), jy = cart_exp(LB, j, 1), jz = cart_exp(LB, j, 2);
+                    const double* Ex = gb + 2;
+                    const double* Ey = Ex + G1B;
+                    const double* Ez = Ey + G1B;
+                    double s = 0.0;
+                    for (int w_ = 0; w_ <= iz + jz; ++w_)
+                        for (int u = 0; u <= iy + jy; ++u)
+                        {
+                            const double eyz = e1(Ey, LB, LAB, iy, jy, u) * e1(Ez, LB, LAB, iz, jz, w_);
+                            for (int t = 0; t <= ix + jx; ++t)
+                                s += eyz * e1(Ex, LB, LAB, ix, jx, t) * Ridx(t + ta, u + nu, w_ + ph);
+                        }
+                    Xs[e] = s;
+                }
+                __syncwarp();
+                // Bra centres A, B.
+                for (int e = lane; e < NAB * HAB1; e += 32)
+                {
+                    const int ij = e / HAB1, h = e % HAB1;
+                    double y = 0.0;
+                    for (int kl = 0; kl < NCD; ++kl) y += Gam[ij * NCD + kl] * Gs[h * NCD + kl];
+                    if (y == 0.0)
+                        continue;
+                    const int tuv = tabs->htuv[LAB + 1][h];
+                    const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
+                    const int i = ij / NB, j = ij % NB;
+                    const int ie[3] = {cart_exp(LA, i, 0), cart_exp(LA, i, 1), cart_exp(LA, i, 2)};
+                    const int je[3] = {cart_exp(LB, j, 0), cart_exp(LB, j, 1), cart_exp(LB, j, 2)};
+                    const double* E[3] = {gb + 2, gb + 2 + G1B, gb + 2 + 2 * G1B};
+                    double f[3], dA[3], dB[3];
+                    for (int x = 0; x < 3; ++x)
+                    {
+                        const int t = tt[x];
+                        f[x]  = (t <= ie[x] + je[x]) ? e1(E[x], LB, LAB, ie[x], je[x], t) : 0.0;
+                        dA[x] = 2.0 * aexp * e1(E[x], LB, LAB, ie[x] + 1, je[x], t) -
+                                (ie[x] > 0 ? ie[x] * e1(E[x], LB, LAB, ie[x] - 1, je[x], t) : 0.0);
+                        dB[x] = 2.0 * bexp * e1(E[x], LB, LAB, ie[x], je[x] + 1, t) -
+                                (je[x] > 0 ? je[x] * e1(E[x], LB, LAB, ie[x], je[x] - 1, t) : 0.0);
+                    }
+                    gA[0] += y * dA[0] * f[1] * f[2];
+                    gA[1] += y * f[0] * dA[1] * f[2];
+                    gA[2] += y * f[0] * f[1] * dA[2];
+                    gB[0] += y * dB[0] * f[1] * f[2];
+                    gB[1] += y * f[0] * dB[1] * f[2];
+                    gB[2] += y * f[0] * f[1] * dB[2];
+                }
+                // Ket centre C.
+                for (int e = lane; e < NCD * HCD1; e += 32)
+                {
+                    const int kl = e / HCD1, h = e % HCD1;
+                    double hv = 0.0;
+                    for (int ij = 0; ij < NAB; ++ij) hv += Gam[ij * NCD + kl] * Xs[ij * HCD1 + h];
+                    if (hv == 0.0)
+                        continue;
+                    const int tuv = tabs->htuv[LCD + 1][h];
+                    const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
+                    if ((tt[0] + tt[1] + tt[2]) & 1)
+                        hv = -hv;
+                    const int k = kl / ND, l = kl % ND;
+                    const int ke[3] = {cart_exp(LC, k, 0), cart_exp(LC, k, 1), cart_exp(LC, k, 2)};
+                    const int le[3] = {cart_exp(LD, l, 0), cart_exp(LD, l, 1), cart_exp(LD, l, 2)};
+                    const double* E[3] = {gk + 2, gk + 2 + G1K, gk + 2 + 2 * G1K};
+                    double f[3], dC[3];
+                    for (int x = 0; x < 3; ++x)
+                    {
+                        const int t = tt[x];
+                        f[x]  = (t <= ke[x] + le[x]) ? e1(E[x], LD, LCD, ke[x], le[x], t) : 0.0;
+                        dC[x] = 2.0 * cexp * e1(E[x], LD, LCD, ke[x] + 1, le[x], t) -
+                                (ke[x] > 0 ? ke[x] * e1(E[x], LD, LCD, ke[x] - 1, le[x], t) : 0.0);
+                    }
+                    gC[0] += hv * dC[0] * f[1] * f[2];
+                    gC[1] += hv * f[0] * dC[1] * f[2];
+                    gC[2] += hv * f[0] * f[1] * dC[2];
+                }
+                __syncwarp();
+            }
+        }
+        for (int x = 0; x < 3; ++x)
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                gA[x] += __shfl_down_sync(0xffffffffu, gA[x], o);
+                gB[x] += __shfl_down_sync(0xffffffffu, gB[x], o);
+                gC[x] += __shfl_down_sync(0xffffffffu, gC[x], o);
+            }
+        if (lane == 0)
+        {
+            const int ta = v.shell_atom[bra.sh1], tb = v.shell_atom[bra.sh2];
+            const int tc = v.shell_atom[ket.sh1], td = v.shell_atom[ket.sh2];
+            for (int x = 0; x < 3; ++x)
+            {
+                atomicAdd(v.grad + 3 * ta + x, gA[x]);
+                atomicAdd(v.grad + 3 * tb + x, gB[x]);
+                atomicAdd(v.grad + 3 * tc + x, gC[x]);
+                atomicAdd(v.grad + 3 * td + x, -(gA[x] + gB[x] + gC[x]));
+            }
+        }
+        __syncwarp();
+    }
+}
+#endif
+} // namespace hfg

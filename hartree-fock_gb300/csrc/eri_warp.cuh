@@ -25,11 +25,12 @@ struct WarpTables
 {
     // Recursion steps per total L (0..kMaxLt), entries in ascending degree order, hidx(.,L) layout:
     // x = dst, y = src1, z = src2 (-1 if absent), w = axis | (coef << 2).
-    int4 rtab[kMaxLt + 1][nherm(kMaxLt)];
+    // (Totals up to kMaxLt + 1: the gradient needs one order more than the Fock build.)
+    int4 rtab[kMaxLt + 2][nherm(kMaxLt + 1)];
     // (t,u,v) of the h-th Hermite index for total L: t | u << 8 | v << 16.
-    int htuv[kMaxLt + 1][nherm(kMaxLt)];
+    int htuv[kMaxLt + 2][nherm(kMaxLt + 1)];
     // hidx(t,u,v,L) from the cube index (t*(L+1)+u)*(L+1)+v.
-    short cube[kMaxLt + 1][(kMaxLt + 1) * (kMaxLt + 1) * (kMaxLt + 1)];
+    short cube[kMaxLt + 2][(kMaxLt + 2) * (kMaxLt + 2) * (kMaxLt + 2)];
     // Per pair class and Cartesian pair ij: x,y,z = lengths of the 1-D Hermite ranges, w = offset of
     // the ij block inside the primitive-pair record (including the header).
     int4 e3[kNumPairClasses][ncart(kMaxL) * ncart(kMaxL)];
@@ -37,7 +38,7 @@ struct WarpTables
 
 inline void build_warp_tables(WarpTables& T)
 {
-    for (int L = 0; L <= kMaxLt; ++L)
+    for (int L = 0; L <= kMaxLt + 1; ++L)
     {
         int k = 0;
         for (int d = 0; d <= L; ++d)

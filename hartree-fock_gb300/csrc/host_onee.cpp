@@ -22,7 +22,7 @@ namespace
 struct HostBoys
 {
     static constexpr double kStep = 0.05;
-    static constexpr int kTerms = 7, kOrders = 2 * kMaxL + 1 + kTerms, kPoints = 602;
+    static constexpr int kTerms = 7, kOrders = 2 * kMaxL + 3 + kTerms, kPoints = 602; // L <= 2 l_max + 2
     std::vector<double> g; // [point][order], orders 0..kOrders-1
     HostBoys() : g(static_cast<size_t>(kPoints) * kOrders)
     {
@@ -76,6 +76,13 @@ const HostBoys& host_boys()
     static const HostBoys b;
     return b;
 }
+} // namespace
+
+// F_0..F_L(T) on the host, L <= 2 l_max + 2 (used by the gradient code as well).
+void host_boys_eval(int L, double T, double* F) { host_boys().eval(L, T, F); }
+
+namespace
+{
 
 constexpr int kE1 = kMaxL + 3; // ket exponent range up to l + 2 for the kinetic integral
 

@@ -59,6 +59,12 @@ class ScfOptions(ctypes.Structure):
                 ("verbose", ctypes.c_int)]
 
 
+class GradRequest(ctypes.Structure):
+    _fields_ = [("natom", ctypes.c_int), ("Z", ctypes.POINTER(ctypes.c_int)), ("xyz", ctypes.POINTER(ctypes.c_double)),
+                ("unrestricted", ctypes.c_int), ("D_alpha", ctypes.c_void_p), ("D_beta", ctypes.c_void_p),
+                ("W", ctypes.c_void_p), ("schwartz_threshold", ctypes.c_double), ("density_threshold", ctypes.c_double)]
+
+
 class ScfResult(ctypes.Structure):
     _fields_ = [("e_electronic", ctypes.c_double), ("e_nuclear", ctypes.c_double), ("e_total", ctypes.c_double),
                 ("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("delta_e", ctypes.c_double),
@@ -103,6 +109,7 @@ def lib():
         L.hfg_core_guess.argtypes = [vp, ctypes.POINTER(ScfOptions), ip, ctypes.POINTER(ctypes.c_int), dpp, ip, ip,
                                      dpp, dpp]
         L.hfg_measure_fma_peak.argtypes = [ip, ip, dpp]
+        L.hfg_gradient.argtypes = [vp, ctypes.POINTER(GradRequest), dpp, dpp]
         _lib = L
     return _lib
 
@@ -183,7 +190,7 @@ class Engine:
         Q = np.asfortranarray(Q, dtype=np.float64).ravel(order="F")
         self._check(lib().hfg_set_schwartz(self.h, _dp(Q)))
 
-    def fock(self, dD_tot, dD_alpha, dD_beta=None, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-6):
+    def fock(self, dD_tot, dD_alpha, dD_beta=None, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-4):
         """(J, Ka, Kb or None, stats dict) for host numpy matrices (single molecule: n x n)."""
         uhf = dD_beta is not None
         flat = lambda x: np.asfortranarray(x, dtype=np.float64).ravel(order="F")
@@ -200,7 +207,7 @@ class Engine:
             outs = [o.reshape(n, n, order="F") if o is not None else None for o in outs]
         return outs[0], outs[1], outs[2], st.as_dict()
 
-    def fock_device(self, ptrs: dict, unrestricted=False, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-6):
+    def fock_device(self, ptrs: dict, unrestricted=False, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-4):
         """Same on device pointers (ints): keys dD_tot, dD_alpha, dD_beta, J, K_alpha, K_beta."""
         g = lambda k: ptrs.get(k) or None
         req = _Request(1 if unrestricted else 0, precision, 1, sthr, dthr, fp32_cutoff, g("dD_tot"), g("dD_alpha"),
@@ -246,6 +253,20 @@ class Engine:
                                          _dp(X), charge, multiplicity, _dp(Da), _dp(Db)))
         return Da, Db
 
+    def gradient(self, Z, xyz, Da=None, Db=None, W=None, unrestricted=False, sthr=1e-10, dthr=1e-10):
+        """Nuclear gradient (natom x 3, Eh/bohr) and the two-electron device time in ms.  With Da None the
+        densities of this engine's last scf() are used (the backward half of scf())."""
+        Zc = np.ascontiguousarray(Z, dtype=np.int32)
+        X = np.ascontiguousarray(xyz, dtype=np.float64)
+        arrs = [np.asfortranarray(m, dtype=np.float64) if m is not None else None for m in (Da, Db, W)]
+        ptr = lambda m: m.ctypes.data if m is not None else None
+        req = GradRequest(len(Zc), Zc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(X), 1 if unrestricted else 0,
+                          *[ptr(m) for m in arrs], sthr, dthr)
+        g = np.zeros((len(Zc), 3))
+        ms = ctypes.c_double()
+        self._check(lib().hfg_gradient(self.h, ctypes.byref(req), _dp(g), ctypes.byref(ms)))
+        return g, ms.value
+
     def eri_block(self, a, b, c, d):
         ls = self._keep[0].a["l"]
         n = [(int(ls[s]) + 1) * (int(ls[s]) + 2) // 2 for s in (a, b, c, d)]
@@ -277,7 +298,7 @@ def measure_fma_peak(fp64: bool, device: int = 0) -> float:
     return t.value
 
 
-def run_input(text: str, precision: int = FP64, fp32_cutoff: float = 1e-6, full_rebuild_every: int = 0,
+def run_input(text: str, precision: int = FP64, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0,
               basis_dir: str | None = None, device: int = 0):
     """Runs a reference-format input end to end: parse, pack the basis, GPU direct SCF."""
     from . import basis as _basis, inputs as _inputs

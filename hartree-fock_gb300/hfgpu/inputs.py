@@ -86,7 +86,7 @@ def parse(text: str) -> JobInput:
     return JobInput(charge, mult, Z, xyz, blocks["basis"][0], scf)
 
 
-def scf_options(job: JobInput, precision: int = 0, fp32_cutoff: float = 1e-6, full_rebuild_every: int = 0) -> dict:
+def scf_options(job: JobInput, precision: int = 0, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0) -> dict:
     """The hfg_scf_options fields for a parsed job, with the reference's defaults."""
     s = job.scf
     max_iter = s.get("max_iter", 30)

@@ -161,7 +161,7 @@ typedef struct hfg_scf_options
     double schwartz_threshold; /* SCHWARTZ_THRESH (1e-10) */
     double density_threshold;  /* DENSITY_THRESH (1e-10) */
     int precision;             /* HFG_PRECISION_FP64 / HFG_PRECISION_MIXED */
-    double fp32_cutoff;        /* FP32 cutoff of the mixed mode (1e-6) */
+    double fp32_cutoff;        /* FP32 cutoff of the mixed mode (1e-4) */
     int full_rebuild_every;    /* 0: incremental builds as the reference; k > 0: full build every k iterations */
     int verbose;               /* print the iteration table to stdout */
 } hfg_scf_options;
@@ -190,6 +190,31 @@ int hfg_scf_run(hfg_engine* engine, const hfg_scf_options* opt, int natom, const
 /* Core-Hamiltonian guess densities (src/SCF.cpp:165-231), host output. */
 int hfg_core_guess(hfg_engine* engine, const hfg_scf_options* opt, int natom, const int* Z, const double* xyz,
                    int charge, int multiplicity, double* D_alpha, double* D_beta);
+
+/* Analytic nuclear gradient (no reference counterpart: the reference has no gradients; checked against
+ * central finite differences of its energy).  The backward half of the forward/backward pair whose
+ * forward half is hfg_scf_run: with D_alpha == NULL the densities and energy-weighted density of the
+ * last hfg_scf_run on this engine are used.  grad: natom x 3 (Eh/bohr).  Two-electron part on the GPU
+ * (FP64 adjoint kernel, E/R tables recomputed), one-electron, overlap and nuclear-repulsion parts FP64 on
+ * the host.  The engine must hold one molecule whose shell centres are the nuclei at xyz. */
+typedef struct hfg_gradient_request
+{
+    int natom;
+    const int* Z;
+    const double* xyz;
+    int unrestricted;
+    const double* D_alpha; /* host, or NULL: use the last SCF's */
+    const double* D_beta;  /* host (UHF; RHF: ignored, D_beta = D_alpha) */
+    const double* W;       /* host: total energy-weighted density sum_s C_occ eps_occ C_occ^T */
+    double schwartz_threshold;
+    double density_threshold;
+} hfg_gradient_request;
+
+int hfg_gradient(hfg_engine* engine, const hfg_gradient_request* req, double* grad, double* ms_two_electron);
+
+/* One-electron, overlap (-W dS) and nuclear-repulsion parts of the gradient, added into grad (host). */
+int hfg_gradient_one_electron(const hfg_basis* basis, const int* shell_atom, int natom, const int* Z,
+                              const double* xyz, const double* D, const double* W, double* grad);
 
 /* Peak FMA throughput of this GPU measured by a register-only FMA loop (TFLOP/s, FP64 if fp64 != 0,
  * else FP32): the denominator of the ERI kernels' roofline. */
