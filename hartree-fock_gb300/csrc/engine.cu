@@ -293,7 +293,7 @@ __global__ void build_lists_kernel(BuildArgs a)
     const long long dthr = __double_as_longlong(a.dthr);
     const long long ra = so + (long long)sa * ns, rb2 = so + (long long)sb * ns;
     const float Qfi = a.Qf1[i];
-    const float dabf = 2.0f * a.Mtf[so + sa + (long long)sb * ns];
+    const float dabf = a.mixed ? 2.0f * a.Mtf[so + sa + (long long)sb * ns] : 0.0f; // FP32 copies exist in mixed mode only
     unsigned c64 = 0, c32 = 0;
     unsigned long long p64 = 0, p32 = 0;
     const unsigned long long o64 = a.pass ? a.bra_off[2 * i] : 0ull;
