@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <stdexcept>
 #include <string>
@@ -1260,6 +1261,49 @@ double flops_per_quartet_digest(int qc, bool uhf)
 }
 } // namespace hfg
 
+
+// ------------------------------------------------------------------------------------------------
+// Allocation-free shell-quartet block.  hfg_eri_block grows a device buffer for every request and
+// frees it afterwards, and cudaFree synchronises the whole device; callers that must not allocate or
+// free device memory per request (a process that runs under a fixed device-memory budget once its
+// engine exists, or a pipeline whose other streams must not be stalled by an implicit device-wide
+// synchronisation) use hfg_eri_block_noalloc instead.  Its scratch -- the one-entry quartet list, the
+// list length and the output block -- lives in this file-scope device array; every GPU that loads the
+// library holds it until the process exits.
+// ------------------------------------------------------------------------------------------------
+namespace hfg
+{
+namespace
+{
+constexpr size_t kNoAllocScratchBytes = 16384;         // stated maximum
+constexpr size_t kNoAllocBlockOffset  = 256;           // Quartet at 0, count at 8, block from 256
+constexpr size_t kNoAllocMaxBlock     = (kNoAllocScratchBytes - kNoAllocBlockOffset) / sizeof(double); // 2016 values
+static __device__ __align__(256) unsigned char hfg_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (set-up once per device, with that device
+// current; the host-side symbol itself is not a device address).
+void* noalloc_scratch(int device)
+{
+    if (device < 0 || device >= kMaxDevices)
+        throw HfgError(HFG_ERR_INVALID, "hfg_eri_block_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device])
+    {
+        void* ptr = nullptr;
+        const cudaError_t rc = cudaGetSymbolAddress(&ptr, hfg_noalloc_scratch);
+        if (rc != cudaSuccess || ptr == nullptr)
+            throw HfgError(HFG_ERR_CUDA, std::string("hfg_eri_block_noalloc: cudaGetSymbolAddress failed: ") +
+                                             cudaGetErrorString(rc));
+        g_noalloc_ptr[device] = ptr;
+    }
+    return g_noalloc_ptr[device];
+}
+} // namespace
+} // namespace hfg
 // ------------------------------------------------------------------------------------------------
 // C ABI.
 // ------------------------------------------------------------------------------------------------
@@ -1543,6 +1587,81 @@ int hfg_gradient(hfg_engine* e, const hfg_gradient_request* r, double* grad, dou
         const int rc = hfg_gradient_one_electron(&hb.view, shell_atom.data(), r->natom, r->Z, r->xyz, Dt.data(), W, grad);
         if (rc != HFG_OK)
             throw HfgError(rc, "hfg_gradient: one-electron part failed");
+    });
+}
+
+int hfg_eri_block_noalloc(hfg_engine* e, int a, int b, int c, int d, double* out)
+{
+    if (!e || !out || e->nmol != 1)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        const int ns = e->mols[0].nshells;
+        if (a < 0 || b < 0 || c < 0 || d < 0 || a >= ns || b >= ns || c >= ns || d >= ns)
+            throw HfgError(HFG_ERR_INVALID, "hfg_eri_block_noalloc: shell index out of range");
+        const auto& hb = e->basis[0];
+        const int na = hfg::ncart(hb.l[a]), nb = hfg::ncart(hb.l[b]), nc = hfg::ncart(hb.l[c]), nd = hfg::ncart(hb.l[d]);
+        const size_t nblk = static_cast<size_t>(na) * nb * nc * nd;
+        if (nblk > hfg::kNoAllocMaxBlock)
+            throw HfgError(HFG_ERR_INVALID, "hfg_eri_block_noalloc: block of " + std::to_string(nblk) +
+                                                " values exceeds the scratch maximum of " +
+                                                std::to_string(hfg::kNoAllocMaxBlock));
+        unsigned char* scratch = static_cast<unsigned char*>(hfg::noalloc_scratch(e->device));
+        auto pair_id = [&](int x, int y) { const int hi = std::max(x, y), lo = std::min(x, y); return hi * (hi + 1) / 2 + lo; };
+        const int pb = pair_id(a, b), pk = pair_id(c, d);
+        const int cb = e->pair_class_of[pb], ck = e->pair_class_of[pk];
+        int bra = pb, ket = pk;
+        if (cb < ck)
+            std::swap(bra, ket);
+        const int qc = hfg::qclass_of(cb, ck);
+        const int P1 = std::max(cb, ck), P2 = std::min(cb, ck);
+        // The one-entry list and its length: written fresh by every call (nothing accumulates in the
+        // scratch; the kernel overwrites every value of the block).
+        struct Head
+        {
+            hfg::Quartet q;
+            unsigned long long n;
+        } head {hfg::Quartet {static_cast<uint32_t>(bra), static_cast<uint32_t>(ket)}, 1ull};
+        HFG_CUDA(cudaMemcpyAsync(scratch, &head, sizeof(head), cudaMemcpyHostToDevice, e->stream));
+        hfg::ClassLaunch L {};
+        L.list        = reinterpret_cast<const hfg::Quartet*>(scratch);
+        L.count_dev   = reinterpret_cast<const unsigned long long*>(scratch + offsetof(Head, n));
+        L.count_host  = 1;
+        L.view        = hfg::base_view(e, false);
+        L.view.store  = reinterpret_cast<double*>(scratch + hfg::kNoAllocBlockOffset);
+        L.view.ao_thr = 0.0;
+        L.boys_slice  = e->d_boys64[hfg::pair_class_l1(P1) + hfg::pair_class_l2(P1) + hfg::pair_class_l1(P2) +
+                                   hfg::pair_class_l2(P2)].p;
+        L.tables      = e->d_tables.p;
+        L.stream      = e->stream;
+        L.num_sms     = e->num_sms;
+        HFG_CUDA(hfg::launch_class(qc, L));
+        double blk[hfg::kNoAllocMaxBlock];
+        HFG_CUDA(cudaMemcpyAsync(blk, scratch + hfg::kNoAllocBlockOffset, sizeof(double) * nblk, cudaMemcpyDeviceToHost,
+                                 e->stream));
+        HFG_CUDA(cudaStreamSynchronize(e->stream));
+        const auto& B = e->pairs[bra];
+        const auto& K = e->pairs[ket];
+        const int n2 = hfg::ncart(hb.l[B.sh2]), n3 = hfg::ncart(hb.l[K.sh1]), n4 = hfg::ncart(hb.l[K.sh2]);
+        const int sh[4] = {a, b, c, d};
+        const bool swap_pairs = (bra != pb);
+        const int p0 = swap_pairs ? 2 : 0, p1 = swap_pairs ? 0 : 2;
+        for (int i = 0; i < na; ++i)
+            for (int j = 0; j < nb; ++j)
+                for (int k = 0; k < nc; ++k)
+                    for (int l = 0; l < nd; ++l)
+                    {
+                        const int cc[4] = {i, j, k, l};
+                        int comp[4];
+                        auto place = [&](int sa_, int sb_, const hfg::PairRec& pr, int* dst) {
+                            const bool direct = (sh[sa_] == pr.sh1 && sh[sb_] == pr.sh2);
+                            dst[0] = direct ? cc[sa_] : cc[sb_];
+                            dst[1] = direct ? cc[sb_] : cc[sa_];
+                        };
+                        place(p0, p0 + 1, B, comp);
+                        place(p1, p1 + 1, K, comp + 2);
+                        out[((i * nb + j) * nc + k) * nd + l] = blk[((comp[0] * n2 + comp[1]) * n3 + comp[2]) * n4 + comp[3]];
+                    }
     });
 }
 

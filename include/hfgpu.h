@@ -127,6 +127,18 @@ int hfg_survivors(hfg_engine* engine, int* quartets, long long cap, long long* c
  * src/IntegralEngine.cpp:731-992): contracted block, row-major [a][b][c][d], full (no zero pattern). */
 int hfg_eri_block(hfg_engine* engine, int a, int b, int c, int d, double* out);
 
+/* Allocation-free variant of hfg_eri_block (no counterpart in the reference).  For callers that must not
+ * allocate or free device memory per request -- a process that runs under a fixed device-memory budget
+ * once its engine exists, or a pipeline whose other streams must not be stalled (hfg_eri_block grows a
+ * device buffer per call and frees it, and cudaFree synchronises the whole device).  Same kernel and
+ * result as hfg_eri_block (host output, row-major [a][b][c][d]); its scratch is a 16 KB file-scope
+ * device array per GPU (held until the process exits), so one block may hold at most 2016 values
+ * (every s/p/d block fits; larger requests fail with HFG_ERR_INVALID).  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device current: make that first
+ * call before any stream capture.  Calls on one device share the array: calls that overlap on the GPU
+ * (from several host threads or engines at once) race. */
+int hfg_eri_block_noalloc(hfg_engine* engine, int a, int b, int c, int d, double* out);
+
 /* The CUDA stream the engine launches on (a cudaStream_t), for callers that time or order work. */
 void* hfg_stream(hfg_engine* engine);
 
