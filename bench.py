@@ -356,6 +356,8 @@ def gpu_arm(args, dist):
                          "prim_fp64": int(sum(st["prim_quartets_fp64"])), "prim_fp32": int(sum(st["prim_quartets_fp32"]))},
             "device_ms": {"build": st["ms_total"], "lists": st["ms_lists"], "eri_fp64": st["ms_eri_fp64"],
                           "eri_fp32": st["ms_eri_fp32"], "fp64_build": st64["ms_total"]},
+            "kernel_forms": {"legend": "per quartet class 0-20: 1 thread, 2 warp, 3 group, 0 not launched",
+                             "fp64": st["form_fp64"], "fp32": st["form_fp32"], "fp64_only_build": st64["form_fp64"]},
             "roofline": {"bound": "fp64", "kernel": "FP64 ERI class kernels (jk_class*_kernel<double>)",
                          "achieved": ach64, "peak": peak64, "unit": "TFLOP/s", "frac": ach64 / peak64 if peak64 else None,
                          "peak_source": "measured FP64 FMA loop (hfg_measure_fma_peak) on this GPU",

@@ -2,6 +2,7 @@
 // per class with -DHFG_QCLASS=<0..20>, so the 21 classes compile in parallel.
 #include "engine.h"
 #include "eri_grad.cuh"
+#include "eri_group.cuh"
 
 #ifndef HFG_QCLASS
 #error "compile with -DHFG_QCLASS=<quartet class>"
@@ -33,13 +34,42 @@ constexpr bool warp_form(bool fp32)
     return fp32 ? (QC == 14 || QC >= 17) : (QC == 12 || QC == 13 || QC == 14 || QC >= 16);
 }
 constexpr bool kWarp = warp_form(false);
+// The primitive-parallel group form exists for the small, contracted classes (L <= 3, <= 27 integrals).
+constexpr bool kGroup = (L <= 3) && (NAB * NCD <= 27);
+constexpr unsigned form_mask(bool fp32)
+{
+    return (warp_form(fp32) ? (1u << kFormWarp) : (1u << kFormThread)) | (kGroup ? (1u << kFormGroup) : 0u);
+}
 
 template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
 {
     constexpr bool kWarpForm = warp_form(sizeof(Real) == 4);
     if (c.count_host == 0)
         return cudaSuccess;
+    const int form = c.form == 0 ? (kWarpForm ? kFormWarp : kFormThread) : c.form;
+    if (!((form_mask(sizeof(Real) == 4) >> form) & 1u))
+        return cudaErrorInvalidValue;
     const size_t slice_bytes = sizeof(Real) * BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow;
+    if constexpr (kGroup)
+    {
+        if (form == kFormGroup)
+        {
+            auto kern         = jk_class_group_kernel<LA, LB, LC, LD, Real, UHF>;
+            const size_t smem = slice_bytes;
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess)
+                return e;
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+            if (e != cudaSuccess)
+                return e;
+            const unsigned long long need = (c.count_host + 127) / 128; // 4 warps x 32-quartet windows
+            const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+            kern<<<static_cast<unsigned>(need < cap ? need : cap), 128, smem, c.stream>>>(
+                c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
+            return cudaGetLastError();
+        }
+    }
     if constexpr (kWarpForm)
     {
         using W             = WarpLayout<LA, LB, LC, LD, Real>;
@@ -89,6 +119,10 @@ cudaError_t HFG_CAT(launch_class_, HFG_QCLASS)(const ClassLaunch& c)
 }
 
 bool HFG_CAT(class_uses_warp_, HFG_QCLASS)() { return kWarp; }
+unsigned HFG_CAT(class_form_mask_, HFG_QCLASS)(bool fp32)
+{
+    return form_mask(fp32) | (static_cast<unsigned>(warp_form(fp32) ? kFormWarp : kFormThread) << 16);
+}
 
 cudaError_t HFG_CAT(launch_grad_, HFG_QCLASS)(const GradLaunch& c)
 {

@@ -7,6 +7,7 @@ namespace hfg
 #define HFG_DECL(c)                                                                                                    \
     cudaError_t launch_class_##c(const ClassLaunch&);                                                                 \
     cudaError_t launch_grad_##c(const GradLaunch&);                                                                   \
+    unsigned class_form_mask_##c(bool);                                                                              \
     bool class_uses_warp_##c();
 HFG_DECL(0) HFG_DECL(1) HFG_DECL(2) HFG_DECL(3) HFG_DECL(4) HFG_DECL(5) HFG_DECL(6) HFG_DECL(7) HFG_DECL(8)
 HFG_DECL(9) HFG_DECL(10) HFG_DECL(11) HFG_DECL(12) HFG_DECL(13) HFG_DECL(14) HFG_DECL(15) HFG_DECL(16)
@@ -42,6 +43,24 @@ cudaError_t launch_class(int qclass, const ClassLaunch& L)
     if (qclass < 0 || qclass >= kNumQuartetClasses)
         return cudaErrorInvalidValue;
     return kLaunch[qclass](L);
+}
+
+static unsigned (*const kMask[kNumQuartetClasses])(bool) = {
+    class_form_mask_0,  class_form_mask_1,  class_form_mask_2,  class_form_mask_3,  class_form_mask_4,
+    class_form_mask_5,  class_form_mask_6,  class_form_mask_7,  class_form_mask_8,  class_form_mask_9,
+    class_form_mask_10, class_form_mask_11, class_form_mask_12, class_form_mask_13, class_form_mask_14,
+    class_form_mask_15, class_form_mask_16, class_form_mask_17, class_form_mask_18, class_form_mask_19,
+    class_form_mask_20};
+
+// The class TUs return the compiled-form mask in bits 0-15 and the default form in bits 16-23.
+unsigned class_form_mask(int qclass, bool fp32)
+{
+    return (qclass >= 0 && qclass < kNumQuartetClasses) ? (kMask[qclass](fp32) & 0xffffu) : 0u;
+}
+
+int class_default_form(int qclass, bool fp32)
+{
+    return (qclass >= 0 && qclass < kNumQuartetClasses) ? static_cast<int>((kMask[qclass](fp32) >> 16) & 0xffu) : 0;
 }
 
 bool class_uses_warp_kernel(int qclass) { return qclass >= 0 && qclass < kNumQuartetClasses && kWarp[qclass](); }

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -120,6 +121,13 @@ struct hfg_engine
     hfg::DevBuf<hfg::PairRec> d_pairs;
     hfg::DevBuf<double> d_pptab64[hfg::kNumPairClasses];
     hfg::DevBuf<float> d_pptab32[hfg::kNumPairClasses];
+    // Field-major copies of the same records (thread kernels' ket reads), field stride kfs[pc].
+    hfg::DevBuf<double> d_ksoa64[hfg::kNumPairClasses];
+    hfg::DevBuf<float> d_ksoa32[hfg::kNumPairClasses];
+    long long kfs[hfg::kNumPairClasses] {};
+    // Host records in pack order: pair k's primitives start at record orig_off[k] of h_tab[class].
+    std::vector<double> h_tab[hfg::kNumPairClasses];
+    std::vector<int> orig_off;
     hfg::DevBuf<long long> d_mat_off;
     hfg::DevBuf<int> d_mat_ld;
     hfg::DevBuf<long long> d_smax_off; // per molecule offset of its shell-max block
@@ -174,6 +182,14 @@ struct hfg_engine
     hfg::DevBuf<hfg::Quartet> d_tmp_list;
     hfg::DevBuf<unsigned long long> d_tmp_count;
 
+    // Kernel forms: the caller's setting per (class, precision), and the pick per (class, precision, UHF).
+    int form_set[hfg::kNumQuartetClasses][2] {};
+    int form_pick[hfg::kNumQuartetClasses][2][2] {};
+    hfg::DevBuf<hfg::Quartet> d_tune_list;
+    hfg::DevBuf<unsigned long long> d_tune_cnt;
+    hfg::DevBuf<double> d_tune_acc[3];
+    cudaEvent_t tune_ev[2] {};
+
     bool last_valid = false;
     int last_mixed  = 0;
 };
@@ -189,6 +205,19 @@ __global__ void to_float_kernel(const double* __restrict__ a, float* __restrict_
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         b[i] = static_cast<float>(a[i]);
+}
+
+// nch contiguous chunks of `chunk` entries, chunk c starting at entry c * (n / nch) of list[0, n)
+// (chunk <= n / nch), and their total count.
+__global__ void sample_list_kernel(const Quartet* __restrict__ list, unsigned long long n, unsigned long long nch,
+                                   unsigned long long chunk, Quartet* __restrict__ out, unsigned long long* __restrict__ count)
+{
+    const unsigned long long m = nch * chunk, step = n / nch;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < m;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        out[i] = list[(i / chunk) * step + i % chunk];
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        *count = m;
 }
 
 // Shell-pair maxima of |dD| (SCF.cpp:544-575) for every molecule block, with exact integer operations
@@ -598,6 +627,40 @@ void hermite_1d(int l1, int l2, double p, double PA, double PB, double E[kMaxL +
 }
 } // namespace
 
+// Uploads the pairs and both layouts of the primitive-pair tables for the current pp_off numbering.
+static void upload_pair_tables(hfg_engine* e)
+{
+    using namespace hfg;
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        const int stride      = pp_stride(pair_class_l1(pc), pair_class_l2(pc));
+        const size_t total    = e->h_tab[pc].size() / stride;
+        const size_t ks       = std::max<size_t>(32, (total + 31) / 32 * 32);
+        std::vector<double> aos(total * stride), soa(ks * stride, 0.0);
+        for (size_t k = 0; k < e->pairs.size(); ++k)
+        {
+            if (e->pair_class_of[k] != pc)
+                continue;
+            const PairRec& pr = e->pairs[k];
+            for (int i = 0; i < pr.npp; ++i)
+            {
+                const double* src = &e->h_tab[pc][static_cast<size_t>(e->orig_off[k] + i) * stride];
+                const size_t slot = static_cast<size_t>(pr.pp_off + i);
+                std::copy(src, src + stride, &aos[slot * stride]);
+                for (int f = 0; f < stride; ++f) soa[f * ks + slot] = src[f];
+            }
+        }
+        e->d_pptab64[pc].upload(aos, e->stream);
+        e->d_pptab32[pc].upload(std::vector<float>(aos.begin(), aos.end()), e->stream);
+        e->d_ksoa64[pc].upload(soa, e->stream);
+        e->d_ksoa32[pc].upload(std::vector<float>(soa.begin(), soa.end()), e->stream);
+        e->kfs[pc] = static_cast<long long>(ks);
+    }
+    e->d_pairs.upload(e->pairs, e->stream);
+    HFG_CUDA(cudaStreamSynchronize(e->stream)); // the host vectors above die here
+    e->have_gtab = false;                       // gradient records follow pp_off too
+}
+
 // Builds pairs, primitive-pair tables and sorted class lists skeleton (without Q).
 static void pack_molecules(hfg_engine* e)
 {
@@ -667,17 +730,13 @@ static void pack_molecules(hfg_engine* e)
                         tab[pc].insert(tab[pc].end(), rec.begin(), rec.end());
                     }
                 class_npp[pc] += pr.npp;
+                e->orig_off.push_back(pr.pp_off);
                 e->pairs.push_back(pr);
                 e->pair_class_of.push_back(pc);
             }
     }
-    e->d_pairs.upload(e->pairs, e->stream);
-    for (int pc = 0; pc < kNumPairClasses; ++pc)
-    {
-        e->d_pptab64[pc].upload(tab[pc], e->stream);
-        std::vector<float> f(tab[pc].begin(), tab[pc].end());
-        e->d_pptab32[pc].upload(f, e->stream);
-    }
+    for (int pc = 0; pc < kNumPairClasses; ++pc) e->h_tab[pc] = std::move(tab[pc]);
+    upload_pair_tables(e);
     std::vector<long long> moff;
     std::vector<int> mld;
     for (const auto& mi : e->mols)
@@ -723,7 +782,11 @@ static FockView base_view(hfg_engine* e, bool fp32)
     FockView v {};
     v.pairs = e->d_pairs.p;
     for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
         v.pptab[pc] = fp32 ? static_cast<const void*>(e->d_pptab32[pc].p) : static_cast<const void*>(e->d_pptab64[pc].p);
+        v.ksoa[pc]  = fp32 ? static_cast<const void*>(e->d_ksoa32[pc].p) : static_cast<const void*>(e->d_ksoa64[pc].p);
+        v.kfs[pc]   = e->kfs[pc];
+    }
     v.mat_off = e->d_mat_off.p;
     v.mat_ld  = e->d_mat_ld.p;
     return v;
@@ -832,6 +895,18 @@ static void sort_classes(hfg_engine* e)
         e->d_cls_molseg[pc].upload(e->cls_molseg[pc], e->stream);
     }
     HFG_CUDA(cudaStreamSynchronize(e->stream));
+    // Renumber the primitive slots of every class in sorted-list order: the kets of a quartet list run
+    // along the sorted class list, so their records become neighbours in the field-major tables.
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        int off = 0;
+        for (int id : e->cls_ids[pc])
+        {
+            e->pairs[id].pp_off = off;
+            off += e->pairs[id].npp;
+        }
+    }
+    upload_pair_tables(e);
     e->have_Q  = true;
     e->cap_thr = -1.0; // capacities depend on Q
 }
@@ -980,6 +1055,83 @@ static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double 
     return launches + nspin;
 }
 
+// Kernel form autotuner.  A class whose list has at least kTuneMin quartets and more than one compiled
+// form runs each form on a sample of its real list (same densities, thresholds and Boys slice; scratch
+// accumulators), once to warm up and kTuneReps times timed with events; the fastest form is kept.  The
+// sample is kTuneChunks contiguous runs spread over the list: contiguous, because neighbouring quartets
+// share their bra pair (which sets the digestion's atomic traffic), and spread, because the list is
+// ordered by primitive count.  At most kTuneSample quartets, several waves of the largest grid.
+constexpr unsigned long long kTuneMin    = 1ull << 16;
+constexpr unsigned long long kTuneSample = 1ull << 21;
+constexpr unsigned long long kTuneChunks = 16;
+constexpr int kTuneReps                  = 2;
+
+int pick_form(hfg_engine* e, int qc, int prec, bool uhf, const ClassLaunch& base, double* ms_tune)
+{
+    const int set = e->form_set[qc][prec];
+    if (set != 0)
+        return set;
+    int& pick = e->form_pick[qc][prec][uhf ? 1 : 0];
+    if (pick != 0)
+        return pick;
+    const unsigned mask = class_form_mask(qc, prec == 1);
+    if ((mask & (mask - 1)) == 0) // a single form
+    {
+        for (int f = 1; f < 32; ++f)
+            if (mask == (1u << f))
+                pick = f;
+        return pick;
+    }
+    const unsigned long long n = base.count_host;
+    if (n < kTuneMin)
+        return 0; // too small to time; the default form runs and the class stays untuned
+    const auto t0 = std::chrono::steady_clock::now();
+    const unsigned long long nch   = n <= kTuneSample ? 1 : kTuneChunks;
+    const unsigned long long chunk = n <= kTuneSample ? n : kTuneSample / kTuneChunks;
+    const unsigned long long m     = nch * chunk;
+    cudaStream_t s = base.stream;
+    e->d_tune_list.alloc(m);
+    e->d_tune_cnt.alloc(1);
+    for (int k = 0; k < 3; ++k)
+    {
+        e->d_tune_acc[k].alloc(e->mat_total);
+        HFG_CUDA(cudaMemsetAsync(e->d_tune_acc[k].p, 0, sizeof(double) * e->mat_total, s));
+    }
+    if (!e->tune_ev[0])
+        for (auto& ev : e->tune_ev) HFG_CUDA(cudaEventCreate(&ev));
+    sample_list_kernel<<<grid_for(static_cast<long long>(m), 256, e->num_sms), 256, 0, s>>>(base.list, n, nch, chunk,
+                                                                                              e->d_tune_list.p, e->d_tune_cnt.p);
+    HFG_CUDA(cudaGetLastError());
+    ClassLaunch t = base;
+    t.list        = e->d_tune_list.p;
+    t.count_dev   = e->d_tune_cnt.p;
+    t.count_host  = m;
+    t.view.X      = e->d_tune_acc[0].p;
+    t.view.Ya     = e->d_tune_acc[1].p;
+    t.view.Yb     = e->d_tune_acc[2].p;
+    float best    = 0.f;
+    for (int f = 1; f < 32; ++f)
+    {
+        if (!((mask >> f) & 1u))
+            continue;
+        t.form = f;
+        HFG_CUDA(launch_class(qc, t));
+        HFG_CUDA(cudaEventRecord(e->tune_ev[0], s));
+        for (int rep = 0; rep < kTuneReps; ++rep) HFG_CUDA(launch_class(qc, t));
+        HFG_CUDA(cudaEventRecord(e->tune_ev[1], s));
+        HFG_CUDA(cudaEventSynchronize(e->tune_ev[1]));
+        float ms = 0.f;
+        HFG_CUDA(cudaEventElapsedTime(&ms, e->tune_ev[0], e->tune_ev[1]));
+        if (pick == 0 || ms < best)
+        {
+            best = ms;
+            pick = f;
+        }
+    }
+    *ms_tune += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return pick;
+}
+
 static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats* st)
 {
     if (!(r.schwartz_threshold >= 0.0) || !(r.density_threshold >= 0.0) || !std::isfinite(r.schwartz_threshold) ||
@@ -1026,6 +1178,8 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
 
     int launches = nspin * (mixed ? 2 : 1) + build_lists(e, uhf, mixed, r.schwartz_threshold, r.density_threshold, r.fp32_cutoff);
     const int ncnt = kNumQuartetClasses * 2;
+    int form_ran[kNumQuartetClasses][2] {};
+    double ms_tune = 0.0;
 
     // Class kernels: FP64 lists, then FP32 lists.
     for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
@@ -1058,7 +1212,9 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
             c.uhf        = uhf;
             c.stream     = s;
             c.num_sms    = e->num_sms;
+            c.form       = pick_form(e, qc, prec, uhf, c, &ms_tune);
             HFG_CUDA(launch_class(qc, c));
+            form_ran[qc][prec] = c.form != 0 ? c.form : (class_default_form(qc, prec == 1));
             ++launches;
         }
     }
@@ -1105,6 +1261,12 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
             st->ms_eri_fp32 = ms;
         }
         st->kernel_launches = launches;
+        for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+        {
+            st->form_fp64[qc] = form_ran[qc][0];
+            st->form_fp32[qc] = form_ran[qc][1];
+        }
+        st->ms_tune = ms_tune;
     }
 }
 
@@ -1486,6 +1648,51 @@ int hfg_fock_direct(hfg_engine* e, const hfg_fock_request* req, hfg_fock_stats* 
         HFG_CUDA(cudaSetDevice(e->device));
         hfg::fock_direct(e, *req, stats);
     });
+}
+
+int hfg_set_kernel_form(hfg_engine* e, int qclass, int fp32, int form)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    if (qclass < -1 || qclass >= hfg::kNumQuartetClasses || (fp32 != 0 && fp32 != 1) || form < HFG_FORM_AUTO ||
+        form > HFG_FORM_GROUP)
+    {
+        e->last_error = "set_kernel_form: class, precision or form out of range";
+        return HFG_ERR_INVALID;
+    }
+    const int lo = qclass < 0 ? 0 : qclass, hi = qclass < 0 ? hfg::kNumQuartetClasses : qclass + 1;
+    for (int qc = lo; qc < hi; ++qc)
+    {
+        const bool ok = form == HFG_FORM_AUTO || ((hfg::class_form_mask(qc, fp32 != 0) >> form) & 1u);
+        if (!ok)
+        {
+            if (qclass >= 0)
+            {
+                e->last_error = "set_kernel_form: form not compiled for this class and precision";
+                return HFG_ERR_UNSUPPORTED;
+            }
+            e->form_set[qc][fp32] = HFG_FORM_AUTO;
+            continue;
+        }
+        e->form_set[qc][fp32] = form;
+        if (form == HFG_FORM_AUTO)
+            e->form_pick[qc][fp32][0] = e->form_pick[qc][fp32][1] = 0;
+    }
+    return HFG_OK;
+}
+
+int hfg_kernel_forms(hfg_engine* e, int fp32, int unrestricted, int* forms, unsigned* available)
+{
+    if (!e || !forms || (fp32 != 0 && fp32 != 1))
+        return HFG_ERR_INVALID;
+    for (int qc = 0; qc < hfg::kNumQuartetClasses; ++qc)
+    {
+        const int set = e->form_set[qc][fp32];
+        forms[qc]     = set != 0 ? set : e->form_pick[qc][fp32][unrestricted ? 1 : 0];
+        if (available)
+            available[qc] = hfg::class_form_mask(qc, fp32 != 0);
+    }
+    return HFG_OK;
 }
 
 int hfg_survivors(hfg_engine* e, int* quartets, long long cap, long long* count)

@@ -24,11 +24,18 @@ struct ClassLaunch
     bool uhf;
     cudaStream_t stream;
     int num_sms;
+    int form; // 0: the class's default form, else one of kFormThread / kFormWarp / kFormGroup
 };
+// Kernel forms of a class kernel (eri_jk.cuh, eri_warp.cuh, eri_group.cuh).
+constexpr int kFormThread = 1, kFormWarp = 2, kFormGroup = 3;
 using ClassLauncher = cudaError_t (*)(const ClassLaunch&);
 // Defined in classes.cu (one translation unit per quartet class).
 cudaError_t launch_class(int qclass, const ClassLaunch& L);
 bool class_uses_warp_kernel(int qclass);
+// Bit f set: form f is compiled for this class and precision.
+unsigned class_form_mask(int qclass, bool fp32);
+// The form a launch with form == 0 runs.
+int class_default_form(int qclass, bool fp32);
 
 struct GradView;
 struct GradLaunch

@@ -38,6 +38,10 @@ struct FockView
 {
     const PairRec* pairs;
     const void* pptab[kNumPairClasses]; // per pair class: primitive-pair records (Real of the kernel)
+    // Per pair class: the same records field-major, value f of primitive slot s at [f * kfs + s].  Slots
+    // follow the sorted class lists, so consecutive kets of a list read consecutive addresses.
+    const void* ksoa[kNumPairClasses];
+    long long kfs[kNumPairClasses];
     const void* Dt;                     // dD_tot   (double for FP64 kernels, float for FP32 kernels)
     const void* Da;                     // dD_alpha
     const void* Db;                     // dD_beta (UHF)
@@ -118,11 +122,26 @@ __device__ __forceinline__ void hermite_R(const Real* Fs, Real X, Real Y, Real Z
         });
 }
 
-// Contracted Cartesian integrals of one quartet (without the angular normalisation factors).
-template <int LA, int LB, int LC, int LD, typename Real>
+// Field f of one primitive-pair record: records stored whole (AoS) or field-major (SoA, stride fs).
+template <typename Real, bool SoA> struct RecRef
+{
+    const Real* __restrict__ p;
+    long long fs;
+    __device__ __forceinline__ Real operator[](int f) const
+    {
+        if constexpr (SoA)
+            return p[f * fs];
+        else
+            return p[f];
+    }
+};
+
+// Contracted Cartesian integrals of one quartet (without the angular normalisation factors).  KSoA: the
+// ket table tk is field-major with field stride kfs.
+template <int LA, int LB, int LC, int LD, typename Real, bool KSoA = false>
 __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& ket, const Real* __restrict__ tb,
                                              const Real* __restrict__ tk, const Real* __restrict__ slice,
-                                             Real* acc)
+                                             Real* acc, long long kfs = 0)
 {
     constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
     constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
@@ -141,7 +160,7 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
 
         for (int ik = 0; ik < ket.npp; ++ik)
         {
-            const Real* __restrict__ rk = tk + static_cast<size_t>(ket.pp_off + ik) * SK;
+            const RecRef<Real, KSoA> rk {KSoA ? tk + (ket.pp_off + ik) : tk + static_cast<size_t>(ket.pp_off + ik) * SK, kfs};
             const Real q = rk[0];
             const Real X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
             const Real rs   = hfg_rsqrt(p + q);
@@ -375,8 +394,9 @@ __global__ void __launch_bounds__(128) jk_class_kernel(const Quartet* __restrict
         return;
     stage_boys<Real>(boys_slice, slice);
     constexpr int N = ncart(LA) * ncart(LB) * ncart(LC) * ncart(LD);
-    const Real* tb  = static_cast<const Real*>(v.pptab[pair_class(LA, LB)]);
-    const Real* tk  = static_cast<const Real*>(v.pptab[pair_class(LC, LD)]);
+    const Real* tb      = static_cast<const Real*>(v.pptab[pair_class(LA, LB)]);
+    const Real* tk      = static_cast<const Real*>(v.ksoa[pair_class(LC, LD)]);
+    const long long kfs = v.kfs[pair_class(LC, LD)];
     for (unsigned long long q = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
          q += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
     {
@@ -384,7 +404,7 @@ __global__ void __launch_bounds__(128) jk_class_kernel(const Quartet* __restrict
         const PairRec bra = v.pairs[qt.bra];
         const PairRec ket = v.pairs[qt.ket];
         Real acc[N];
-        eval_quartet<LA, LB, LC, LD, Real>(bra, ket, tb, tk, slice, acc);
+        eval_quartet<LA, LB, LC, LD, Real, true>(bra, ket, tb, tk, slice, acc, kfs);
         if (v.store != nullptr)
         {
             static_for<0, N>(

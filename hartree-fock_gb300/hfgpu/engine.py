@@ -15,6 +15,7 @@ from . import build as _build
 HFG_OK = 0
 FP64, MIXED = 0, 1
 NUM_CLASSES = 21
+FORM_AUTO, FORM_THREAD, FORM_WARP, FORM_GROUP = 0, 1, 2, 3
 
 _lib = None
 
@@ -37,13 +38,16 @@ class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_ulonglong * NUM_CLASSES) for n in
                 ("quartets_fp64", "quartets_fp32", "prim_quartets_fp64", "prim_quartets_fp32")] + [
         (n, ctypes.c_double) for n in ("flops_fp64", "flops_fp32", "ms_total", "ms_lists", "ms_eri_fp64",
-                                       "ms_eri_fp32")] + [("kernel_launches", ctypes.c_int)]
+                                       "ms_eri_fp32")] + [("kernel_launches", ctypes.c_int),
+                                                          ("form_fp64", ctypes.c_int * NUM_CLASSES),
+                                                          ("form_fp32", ctypes.c_int * NUM_CLASSES),
+                                                          ("ms_tune", ctypes.c_double)]
 
     def as_dict(self):
         d = {n: list(getattr(self, n)) for n in ("quartets_fp64", "quartets_fp32", "prim_quartets_fp64",
-                                                 "prim_quartets_fp32")}
+                                                 "prim_quartets_fp32", "form_fp64", "form_fp32")}
         d.update({n: getattr(self, n) for n in ("flops_fp64", "flops_fp32", "ms_total", "ms_lists", "ms_eri_fp64",
-                                                "ms_eri_fp32", "kernel_launches")})
+                                                "ms_eri_fp32", "kernel_launches", "ms_tune")})
         return d
 
 
@@ -97,6 +101,8 @@ def lib():
         L.hfg_fock_direct.argtypes = [vp, ctypes.POINTER(_Request), ctypes.POINTER(Stats)]
         L.hfg_survivors.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
         L.hfg_eri_block.argtypes = [vp, ip, ip, ip, ip, ctypes.POINTER(ctypes.c_double)]
+        L.hfg_set_kernel_form.argtypes = [vp, ip, ip, ip]
+        L.hfg_kernel_forms.argtypes = [vp, ip, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)]
         L.hfg_stream.argtypes = [vp]
         L.hfg_stream.restype = vp
         L.hfg_version.restype = ctypes.c_char_p
@@ -215,6 +221,17 @@ class Engine:
         st = Stats()
         self._check(lib().hfg_fock_direct(self.h, ctypes.byref(req), ctypes.byref(st)))
         return st.as_dict()
+
+    def set_kernel_form(self, form, qclass=-1, fp32=False):
+        """Force a kernel form (FORM_THREAD / FORM_WARP / FORM_GROUP) or return to FORM_AUTO."""
+        self._check(lib().hfg_set_kernel_form(self.h, qclass, 1 if fp32 else 0, form))
+
+    def kernel_forms(self, fp32=False, unrestricted=False):
+        """(forms in use per class, 0 = not tuned yet; bit masks of the compiled forms)."""
+        forms = (ctypes.c_int * NUM_CLASSES)()
+        avail = (ctypes.c_uint * NUM_CLASSES)()
+        self._check(lib().hfg_kernel_forms(self.h, 1 if fp32 else 0, 1 if unrestricted else 0, forms, avail))
+        return list(forms), list(avail)
 
     def survivors(self):
         cnt = ctypes.c_longlong()

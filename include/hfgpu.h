@@ -91,6 +91,9 @@ typedef struct hfg_fock_stats
     double ms_eri_fp64; /* device time of the FP64 class kernels */
     double ms_eri_fp32; /* device time of the FP32 class kernels */
     int kernel_launches;
+    int form_fp64[HFG_NUM_CLASSES]; /* kernel form each class ran in (HFG_FORM_*; 0 = class not launched) */
+    int form_fp32[HFG_NUM_CLASSES];
+    double ms_tune;     /* host wall time spent timing kernel forms in this call (first use of a class only) */
 } hfg_fock_stats;
 
 /* IntegralEngine::IntegralEngine(const BasisSet&) (include/IntegralEngine.hpp:11).  Packs the basis
@@ -117,6 +120,25 @@ int hfg_set_schwartz(hfg_engine* engine, const double* Q);
 
 /* SCF::buildFockMatrixDirect (include/SCF.hpp:129, src/SCF.cpp:523-744); `stats` may be NULL. */
 int hfg_fock_direct(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_stats* stats);
+
+/* Kernel forms of a class kernel.  THREAD: one thread per shell quartet.  WARP: one warp per quartet
+ * (the large d classes).  GROUP: a power-of-two group of lanes per quartet, splitting its primitive
+ * quartets (the small contracted classes, L <= 3).  AUTO: on the first build that runs the class with
+ * enough quartets, every compiled form runs on an evenly spaced sample of the real list and the fastest
+ * is kept for the life of the engine (per class, precision and RHF/UHF).
+ * No reference counterpart: the reference has one CPU loop (src/SCF.cpp:592-728). */
+#define HFG_FORM_AUTO 0
+#define HFG_FORM_THREAD 1
+#define HFG_FORM_WARP 2
+#define HFG_FORM_GROUP 3
+/* Set the form of class `qclass` (-1: every class) at precision `fp32` (0: FP64 kernels, 1: FP32
+ * kernels).  HFG_FORM_AUTO forgets earlier timings; a form the class was not compiled in returns
+ * HFG_ERR_UNSUPPORTED (with qclass -1 such classes keep AUTO). */
+int hfg_set_kernel_form(hfg_engine* engine, int qclass, int fp32, int form);
+/* Forms in use: forms[qc] for the given precision and spin case, 0 where AUTO has not decided yet.
+ * `available` (may be NULL) receives the bit mask of compiled forms per class (bit f = form f). */
+int hfg_kernel_forms(hfg_engine* engine, int fp32, int unrestricted, int forms[HFG_NUM_CLASSES],
+                     unsigned available[HFG_NUM_CLASSES]);
 
 /* The surviving canonical shell quartets (a >= b, c >= d, ab >= cd; the reference's loop indices,
  * SCF.cpp:592-623) of the last hfg_fock_direct call, sorted lexicographically, as 4 ints each.

@@ -1,0 +1,121 @@
+"""Every compiled kernel form of every class gives the reference's Fock matrix, and the form autotuner
+only ever picks a compiled form.
+
+Forms: THREAD (one thread per shell quartet), WARP (one warp per quartet, large d classes), GROUP (a
+power-of-two lane group per quartet splitting its primitive quartets, classes up to L = 3).  Tolerances
+as in test_gpu_fock: FP64 within 1e-10 Eh of the reference, mixed within 1e-6 of FP64.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ["w2_631gss", "w2_cation_uhf_631gss", "w2_ccpvdz"]
+
+
+def _engine(g):
+    from hfgpu.engine import Engine
+
+    return Engine(g["soa"])
+
+
+def _force(e, fp32, pick):
+    """Force, per class, the form `pick(mask)` chooses from the compiled-form mask (None: AUTO)."""
+    from hfgpu.engine import FORM_AUTO
+
+    _, avail = e.kernel_forms(fp32=fp32)
+    for qc, mask in enumerate(avail):
+        f = pick(mask)
+        e.set_kernel_form(FORM_AUTO if f is None else f, qclass=qc, fp32=fp32)
+
+
+def _group_else_default(mask):
+    from hfgpu.engine import FORM_GROUP
+
+    return FORM_GROUP if mask >> FORM_GROUP & 1 else None
+
+
+def _non_group(mask):
+    from hfgpu.engine import FORM_THREAD, FORM_WARP
+
+    return FORM_WARP if mask >> FORM_WARP & 1 else FORM_THREAD
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("which", ["group", "plain"])
+def test_gpu_forced_forms_fp64_match_reference(name, which):
+    g = load_golden(name)
+    e = _engine(g)
+    e.set_schwartz(g["Q"])
+    _force(e, False, _group_else_default if which == "group" else _non_group)
+    uhf = bool(g["unrestricted"])
+    Da, Db = g["Da"], g["Db"]
+    J, Ka, Kb, st = e.fock(Da + Db, Da, Db if uhf else None)
+    assert np.max(np.abs((J - Ka) - g["Fa"])) <= 1e-10
+    if uhf:
+        assert np.max(np.abs((J - Kb) - g["Fb"])) <= 1e-10
+    forms, avail = e.kernel_forms(unrestricted=uhf)
+    for qc, n in enumerate(st["quartets_fp64"]):
+        if n:
+            ran = st["form_fp64"][qc]
+            # 0: AUTO with a list below the tuning size, which runs the class's default form.
+            assert avail[qc] >> ran & 1 and forms[qc] in (0, ran)
+    if which == "group":
+        assert any(f == 3 for f in st["form_fp64"])
+
+
+@pytest.mark.parametrize("name", ["w2_631gss", "w2_cation_uhf_631gss"])
+def test_gpu_forced_group_form_mixed_close_to_fp64(name):
+    g = load_golden(name)
+    e = _engine(g)
+    uhf = bool(g["unrestricted"])
+    Da, Db = g["Da"], g["Db"]
+    J64, K64, _, _ = e.fock(Da + Db, Da, Db if uhf else None)
+    _force(e, False, _group_else_default)
+    _force(e, True, _group_else_default)
+    J32, K32, _, s32 = e.fock(Da + Db, Da, Db if uhf else None, precision=1, fp32_cutoff=1e-4)
+    assert any(f == 3 for f in s32["form_fp32"])
+    assert np.max(np.abs(J32 - J64)) <= 1e-6
+    assert np.max(np.abs(K32 - K64)) <= 1e-6
+
+
+def test_gpu_autotune_picks_compiled_forms():
+    from hfgpu import basis, workloads
+    from hfgpu.engine import Engine
+
+    # (H2O)_16 / 6-31G**: several classes hold more quartets than the tuning threshold.
+    Z, xyz = workloads.water_lattice(4, 2, 2, spacing=5.5, seed=0, jitter=0.2)
+    e = Engine(basis.pack("6-31G**", Z, xyz))
+    Da, _ = e.core_guess(Z, xyz, 0, 1)
+    J0, K0, _, st0 = e.fock(2 * Da, Da)  # AUTO times the forms on this first build
+    assert st0["ms_tune"] > 0.0
+    forms, avail = e.kernel_forms()
+    tuned = [qc for qc, f in enumerate(forms) if f]
+    assert tuned, "no class reached the tuning size"
+    for qc in tuned:
+        assert avail[qc] >> forms[qc] & 1
+    # The tuned build and a second build with the cached picks agree with each other to rounding.
+    J1, K1, _, st = e.fock(2 * Da, Da)
+    assert st["ms_tune"] == 0.0
+    assert np.max(np.abs(J1 - J0)) <= 1e-11 and np.max(np.abs(K1 - K0)) <= 1e-11
+
+
+def test_gpu_set_kernel_form_rejects_uncompiled_form():
+    from hfgpu.engine import FORM_GROUP, FORM_WARP
+
+    g = load_golden("h2o_631g")
+    e = _engine(g)
+    _, avail = e.kernel_forms()
+    assert not (avail[20] >> FORM_GROUP & 1)  # (dd|dd) has no group form
+    with pytest.raises(RuntimeError):
+        e.set_kernel_form(FORM_GROUP, qclass=20)
+    assert not (avail[0] >> FORM_WARP & 1)  # (ss|ss) has no warp form
+    with pytest.raises(RuntimeError):
+        e.set_kernel_form(FORM_WARP, qclass=0)
+    with pytest.raises(RuntimeError):
+        e.set_kernel_form(7, qclass=0)
+    e.set_kernel_form(FORM_GROUP)  # every class: those without a group form stay AUTO
+    forms, _ = e.kernel_forms()
+    assert forms[0] == FORM_GROUP and forms[20] == 0
