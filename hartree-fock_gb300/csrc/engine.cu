@@ -119,6 +119,10 @@ struct hfg_engine
     std::vector<hfg::PairRec> pairs;
     std::vector<int> pair_class_of;
     hfg::DevBuf<hfg::PairRec> d_pairs;
+    // The pairs in sorted-list order (class by class; position k of class pc at cls_base[pc] + k): the
+    // quartet lists hold these indices, so the kets of a warp read neighbouring records.
+    std::vector<int> cls_base, spair_id;
+    hfg::DevBuf<hfg::PairRec> d_spairs;
     hfg::DevBuf<double> d_pptab64[hfg::kNumPairClasses];
     hfg::DevBuf<float> d_pptab32[hfg::kNumPairClasses];
     // Field-major copies of the same records (thread kernels' ket reads), field stride kfs[pc].
@@ -263,7 +267,7 @@ struct BuildArgs
     const int* ids1;
     const double* Q1;
     int n1;
-    const int* ids2;
+    int base1, base2; // sorted-array index of position 0 of each class (what the lists hold)
     const double* Q2;
     const int2* sh2;     // (sh1, sh2) per ket position
     const int4* seg2;    // ket class segments (equal primitive-pair count, Q descending inside)
@@ -349,10 +353,8 @@ __global__ void build_lists_kernel(BuildArgs a)
         {
             const int j = base + lane;
             bool s64 = false, s32 = false;
-            int pid_j = 0;
             if (j < jend)
             {
-                pid_j = a.ids2[j];
                 const int2 scd = a.sh2[j];
                 const int sc = scd.x, sd = scd.y;
                 long long md = max(dab, bits(a.Mt2, so + sc + (long long)sd * ns));
@@ -380,7 +382,7 @@ __global__ void build_lists_kernel(BuildArgs a)
             const unsigned lt  = (1u << lane) - 1u;
             if (a.pass)
             {
-                const Quartet qv {static_cast<uint32_t>(pid_i), static_cast<uint32_t>(pid_j)};
+                const Quartet qv {static_cast<uint32_t>(a.base1 + i), static_cast<uint32_t>(a.base2 + j)};
                 const unsigned long long w64 = o64 + c64 + __popc(m64 & lt), w32 = o32 + c32 + __popc(m32 & lt);
                 if (s64 && w64 < a.cap)
                     a.out64[w64] = qv;
@@ -647,7 +649,8 @@ static void upload_pair_tables(hfg_engine* e)
                 const double* src = &e->h_tab[pc][static_cast<size_t>(e->orig_off[k] + i) * stride];
                 const size_t slot = static_cast<size_t>(pr.pp_off + i);
                 std::copy(src, src + stride, &aos[slot * stride]);
-                for (int f = 0; f < stride; ++f) soa[f * ks + slot] = src[f];
+                const size_t kslot = static_cast<size_t>(pr.kslot) + static_cast<size_t>(i) * pr.kstep;
+                for (int f = 0; f < stride; ++f) soa[f * ks + kslot] = src[f];
             }
         }
         e->d_pptab64[pc].upload(aos, e->stream);
@@ -657,6 +660,9 @@ static void upload_pair_tables(hfg_engine* e)
         e->kfs[pc] = static_cast<long long>(ks);
     }
     e->d_pairs.upload(e->pairs, e->stream);
+    std::vector<PairRec> sp(e->spair_id.size());
+    for (size_t k = 0; k < sp.size(); ++k) sp[k] = e->pairs[e->spair_id[k]];
+    e->d_spairs.upload(sp, e->stream);
     HFG_CUDA(cudaStreamSynchronize(e->stream)); // the host vectors above die here
     e->have_gtab = false;                       // gradient records follow pp_off too
 }
@@ -688,6 +694,8 @@ static void pack_molecules(hfg_engine* e)
                 pr.npp    = b.nprim[a] * b.nprim[bb];
                 pr.mol    = m;
                 pr.same   = (s1 == s2) ? 1 : 0;
+                pr.kslot  = pr.pp_off;
+                pr.kstep  = 1;
                 const double* A = &b.centers[3 * a];
                 const double* B = &b.centers[3 * bb];
                 const double AB2 = (A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) + (A[2] - B[2]) * (A[2] - B[2]);
@@ -895,15 +903,28 @@ static void sort_classes(hfg_engine* e)
         e->d_cls_molseg[pc].upload(e->cls_molseg[pc], e->stream);
     }
     HFG_CUDA(cudaStreamSynchronize(e->stream));
-    // Renumber the primitive slots of every class in sorted-list order: the kets of a quartet list run
-    // along the sorted class list, so their records become neighbours in the field-major tables.
+    // Renumber the primitive slots of every class in sorted-list order.  Whole records (pp_off) stay
+    // contiguous per pair; in the field-major tables a segment of equal primitive count is stored
+    // primitive-major, so the kets of a warp (neighbours in one segment) read neighbouring slots for
+    // every primitive index.
+    e->cls_base.assign(kNumPairClasses, 0);
+    e->spair_id.clear();
     for (int pc = 0; pc < kNumPairClasses; ++pc)
     {
+        e->cls_base[pc] = static_cast<int>(e->spair_id.size());
+        e->spair_id.insert(e->spair_id.end(), e->cls_ids[pc].begin(), e->cls_ids[pc].end());
         int off = 0;
-        for (int id : e->cls_ids[pc])
+        for (const int4& seg : e->cls_seg[pc])
         {
-            e->pairs[id].pp_off = off;
-            off += e->pairs[id].npp;
+            const int seg_off = off, len = seg.y - seg.x;
+            for (int k = seg.x; k < seg.y; ++k)
+            {
+                PairRec& pr = e->pairs[e->cls_ids[pc][k]];
+                pr.pp_off   = off;
+                pr.kslot    = seg_off + (k - seg.x);
+                pr.kstep    = len;
+                off += pr.npp;
+            }
         }
     }
     upload_pair_tables(e);
@@ -996,9 +1017,10 @@ static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double 
                     continue;
                 BuildArgs a {};
                 a.ids1 = e->d_cls_ids[P1].p;
+                a.base1 = e->cls_base[P1];
+                a.base2 = e->cls_base[P2];
                 a.Q1   = e->d_cls_Q[P1].p;
                 a.n1   = static_cast<int>(e->cls_ids[P1].size());
-                a.ids2 = e->d_cls_ids[P2].p;
                 a.Q2   = e->d_cls_Q[P2].p;
                 a.sh2  = e->d_cls_sh[P2].p;
                 a.seg2 = e->d_cls_seg[P2].p;
@@ -1198,6 +1220,7 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
             c.count_dev  = e->d_counts.p + 2 * qc + prec;
             c.count_host = n;
             c.view       = base_view(e, prec == 1);
+            c.view.pairs = e->d_spairs.p;
             c.view.Dt    = prec == 1 ? static_cast<const void*>(e->d_dDf[0].p) : e->d_dD[0].p;
             c.view.Da    = prec == 1 ? static_cast<const void*>(e->d_dDf[1].p) : e->d_dD[1].p;
             c.view.Db    = prec == 1 ? static_cast<const void*>(e->d_dDf[2].p) : e->d_dD[2].p;
@@ -1355,7 +1378,7 @@ static double gradient_two_electron(hfg_engine* e, const std::vector<int>& shell
     size_lists(e, sthr, false);
     build_lists(e, uhf, false, sthr, dthr, 0.0);
     GradView v {};
-    v.pairs = e->d_pairs.p;
+    v.pairs = e->d_spairs.p;
     for (int pc = 0; pc < kNumPairClasses; ++pc)
     {
         v.pptab[pc] = e->d_pptab64[pc].p;
@@ -1714,8 +1737,8 @@ int hfg_survivors(hfg_engine* e, int* quartets, long long cap, long long* count)
                 HFG_CUDA(cudaMemcpy(q.data(), e->d_list[qc][prec].p, sizeof(hfg::Quartet) * n, cudaMemcpyDeviceToHost));
                 for (const auto& x : q)
                 {
-                    const auto& P = e->pairs[x.bra];
-                    const auto& K = e->pairs[x.ket];
+                    const auto& P = e->pairs[e->spair_id[x.bra]];
+                    const auto& K = e->pairs[e->spair_id[x.ket]];
                     int a = std::max(P.sh1, P.sh2), b = std::min(P.sh1, P.sh2);
                     int c = std::max(K.sh1, K.sh2), d = std::min(K.sh1, K.sh2);
                     const long long ab = static_cast<long long>(a) * (a + 1) / 2 + b;

@@ -160,7 +160,9 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
 
         for (int ik = 0; ik < ket.npp; ++ik)
         {
-            const RecRef<Real, KSoA> rk {KSoA ? tk + (ket.pp_off + ik) : tk + static_cast<size_t>(ket.pp_off + ik) * SK, kfs};
+            const RecRef<Real, KSoA> rk {KSoA ? tk + (ket.kslot + static_cast<long long>(ik) * ket.kstep)
+                                              : tk + static_cast<size_t>(ket.pp_off + ik) * SK,
+                                         kfs};
             const Real q = rk[0];
             const Real X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
             const Real rs   = hfg_rsqrt(p + q);

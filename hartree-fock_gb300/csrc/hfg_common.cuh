@@ -136,10 +136,11 @@ struct PairRec
     int npp;          // number of primitive pairs
     int mol;          // molecule (batch) index
     int same;         // 1 if sh1 == sh2
+    int kslot, kstep; // field-major tables: primitive pair i at slot kslot + i * kstep
 };
 
 struct Quartet
 {
-    uint32_t bra, ket; // indices into the pair list; bra's class >= ket's class
+    uint32_t bra, ket; // indices into a pair array (the sorted one for built lists); bra's class >= ket's class
 };
 } // namespace hfg

@@ -92,6 +92,11 @@ def build(verbose: bool = True, jobs: int | None = None) -> str:
     with cf.ThreadPoolExecutor(jobs) as ex:
         results = list(ex.map(_compile, order))
     objs = [o for o, _ in results]
+    # Drop cached objects of earlier source versions.
+    keep = {os.path.basename(o) for o in objs}
+    for name in os.listdir(BUILD_DIR):
+        if name.endswith(".o") and name not in keep:
+            os.remove(os.path.join(BUILD_DIR, name))
     rebuilt = any(b for _, b in results) or not os.path.exists(LIB_PATH)
     if rebuilt:
         cuda_lib = os.path.join(cuda_home(), "lib64")
