@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                         const double xa = ax == 0 ? X : (ax == 1 ? Y : Z);
                         double val    = xa * src[r.y];
                         if (c > 0)
-                            val += double(c) * src[r.z];
+                            val = fma(tabs->rcoef[L][k], src[r.z], val);
                         dst[r.x] = val;
                     }
                     if (lane == 0)
@@ -192,8 +192,8 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                             const double eyz = e1(Ey, LD, LCD, ky, ly, nu) * e1(Ez, LD, LCD, kz, lz, ph);
                             for (int ta = 0; ta <= kx + lx; ++ta)
                             {
-                                const double term = eyz * e1(Ex, LD, LCD, kx, lx, ta) * Ridx(t + ta, u + nu, w_ + ph);
-                                s += ((ta + nu + ph) & 1) ? -term : term;
+                                const double ek = eyz * e1(Ex, LD, LCD, kx, lx, ta);
+                                s = fma(((ta + nu + ph) & 1) ? -ek : ek, Ridx(t + ta, u + nu, w_ + ph), s);
                             }
                         }
                     Gs[e] = s;

@@ -2,9 +2,10 @@
 // (the d-containing classes), where one thread cannot hold the quartet's Hermite and integral arrays
 // in registers.
 //
-// One warp evaluates one quartet.  Per primitive quartet every lane computes the scalar part (T, the
-// prefactor, Boys F_0..F_L) -- the FP64 pipe pays per warp instruction, so this costs no more than one
-// lane doing it -- and the data-parallel parts are spread over the lanes through shared memory:
+// One warp evaluates one quartet.  The scalar part of a primitive quartet (T, the prefactor, Boys
+// F_0..F_L) is computed for 32 primitive quartets at once, one per lane (the FP64 pipe pays per warp
+// instruction, so a scalar computed by every lane for the same primitive quartet would cost as much as
+// 32 distinct ones), and the data-parallel parts are spread over the lanes through shared memory:
 //   * R^n_{tuv}: level by level (n = L-1 .. 0), every entry of a level computed by some lane from the
 //     previous level (ping-pong buffers), the recursion of src/IntegralEngine.cpp:1082-1162;
 //   * G[tuv][kl] (ket Hermite -> Cartesian, summed over ket primitives): each lane owns entries;
@@ -27,6 +28,8 @@ struct WarpTables
     // x = dst, y = src1, z = src2 (-1 if absent), w = axis | (coef << 2).
     // (Totals up to kMaxLt + 1: the gradient needs one order more than the Fock build.)
     int4 rtab[kMaxLt + 2][nherm(kMaxLt + 1)];
+    // The integer coefficient of each step as a double (no int -> double conversion on the FP64 pipe).
+    double rcoef[kMaxLt + 2][nherm(kMaxLt + 1)];
     // (t,u,v) of the h-th Hermite index for total L: t | u << 8 | v << 16.
     int htuv[kMaxLt + 2][nherm(kMaxLt + 1)];
     // hidx(t,u,v,L) from the cube index (t*(L+1)+u)*(L+1)+v.
@@ -78,6 +81,7 @@ inline void build_warp_tables(WarpTables& T)
                         r.z = -1;
                     }
                     r.w             = ax | (c << 2);
+                    T.rcoef[L][k]   = c;
                     T.rtab[L][k++] = r;
                 }
         for (int h = 0; h < nherm(L); ++h)
@@ -104,11 +108,13 @@ template <int LA, int LB, int LC, int LD, typename Real> struct WarpLayout
     static constexpr int NAB = NA * NB, NCD = NC * ND;
     static constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
     static constexpr int HAB = nherm(LAB), HL = nherm(L);
-    // Per-warp shared scratch (in Real units): two R levels, G, and the digested integrals.
+    // Per-warp shared scratch (in Real units): two R levels, G, the digested integrals, and the scalar
+    // part (X, Y, Z, scaled Boys values) of a batch of 32 primitive quartets.
     static constexpr int kR   = 2 * HL;
     static constexpr int kG   = HAB * NCD;
     static constexpr int kE   = NAB * NCD;
-    static constexpr int kPerWarp = ((kR + kG + kE + 1) / 2) * 2;
+    static constexpr int kPb  = 32 * (L + 4);
+    static constexpr int kPerWarp = ((kR + kG + kE + kPb + 1) / 2) * 2;
     static constexpr int kAcc     = (NAB * NCD + 31) / 32;
 };
 
@@ -137,6 +143,7 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
     Real* Rbuf1 = wbase + HL;
     Real* Gs    = wbase + 2 * HL;
     Real* Es    = Gs + W::kG;
+    Real* Pb    = Es + W::kE;
 
     const Real* tb = static_cast<const Real*>(v.pptab[PCB]);
     const Real* tk = static_cast<const Real*>(v.pptab[PCK]);
@@ -151,38 +158,53 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
 #pragma unroll
         for (int m = 0; m < W::kAcc; ++m) acc[m] = Real(0);
 
-        for (int ib = 0; ib < bra.npp; ++ib)
+        // Primitive quartets t = ib * npk + ik in batches of 32: lane j of a batch computes the scalar
+        // part of quartet base + j (T, prefactor, Boys) into the warp's buffer Pb, then the warp walks
+        // the batch, running the distributed recursion and contractions on one primitive quartet at a time.
+        const int npk = ket.npp, P = bra.npp * npk;
+        for (int base = 0; base < P; base += 32)
         {
-            const Real* __restrict__ rb = tb + static_cast<size_t>(bra.pp_off + ib) * SB;
-            const Real p = rb[0], Px = rb[1], Py = rb[2], Pz = rb[3], Wab = rb[4];
-            for (int e = lane; e < W::kG; e += 32) Gs[e] = Real(0);
-            for (int ik = 0; ik < ket.npp; ++ik)
+            __syncwarp(); // the previous batch's reads of Pb are done
             {
-                const Real* __restrict__ rk = tk + static_cast<size_t>(ket.pp_off + ik) * SK;
-                const Real qq = rk[0];
-                const Real X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
-                const Real rs   = hfg_rsqrt(p + qq);
-                const Real rho  = (p * qq) * (rs * rs);
-                const Real pref = (Wab * rk[4]) * rs;
-                const Real T    = rho * (X * X + Y * Y + Z * Z);
-                Real F[L + 1];
-                boys_eval<L, Real>(T, slice, F);
-                Real Fs[L + 1];
+                const int t = base + lane;
+                if (t < P)
                 {
+                    const int ib = t / npk, ik = t - ib * npk;
+                    const Real* __restrict__ rb = tb + static_cast<size_t>(bra.pp_off + ib) * SB;
+                    const Real* __restrict__ rk = tk + static_cast<size_t>(ket.pp_off + ik) * SK;
+                    const Real p = rb[0], qq = rk[0];
+                    const Real X = rb[1] - rk[1], Y = rb[2] - rk[2], Z = rb[3] - rk[3];
+                    const Real rs   = hfg_rsqrt(p + qq);
+                    const Real rho  = (p * qq) * (rs * rs);
+                    const Real pref = (rb[4] * rk[4]) * rs;
+                    const Real T    = rho * (X * X + Y * Y + Z * Z);
+                    Real F[L + 1];
+                    boys_eval<L, Real>(T, slice, F);
+                    Pb[0 * 32 + lane] = X;
+                    Pb[1 * 32 + lane] = Y;
+                    Pb[2 * 32 + lane] = Z;
                     const Real m2r = Real(-2) * rho;
                     Real w         = pref;
 #pragma unroll
                     for (int k = 0; k <= L; ++k)
                     {
-                        Fs[k] = w * F[k];
+                        Pb[(3 + k) * 32 + lane] = w * F[k];
                         w *= m2r;
                     }
                 }
+            }
+            __syncwarp();
+            const int nb = min(32, P - base);
+            for (int j = 0; j < nb; ++j)
+            {
+                const int t = base + j, ib = t / npk, ik = t - ib * npk;
+                const Real X = Pb[0 * 32 + j], Y = Pb[1 * 32 + j], Z = Pb[2 * 32 + j];
+                const Real* __restrict__ rk = tk + static_cast<size_t>(ket.pp_off + ik) * SK;
                 // R recursion, level n+1 in `src`, level n into `dst`.
                 Real* src = Rbuf0;
                 Real* dst = Rbuf1;
                 if (lane == 0)
-                    src[0] = Fs[L];
+                    src[0] = Pb[(3 + L) * 32 + j];
                 __syncwarp();
 #pragma unroll
                 for (int lev = L - 1; lev >= 0; --lev)
@@ -195,23 +217,29 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
                         const Real xa = ax == 0 ? X : (ax == 1 ? Y : Z);
                         Real val      = xa * src[r.y];
                         if (c > 0)
-                            val += Real(c) * src[r.z];
+                        {
+                            if constexpr (sizeof(Real) == 8)
+                                val = fma(tabs->rcoef[L][k], src[r.z], val);
+                            else
+                                val = fmaf(Real(c), src[r.z], val);
+                        }
                         dst[r.x] = val;
                     }
                     if (lane == 0)
-                        dst[0] = Fs[lev];
+                        dst[0] = Pb[(3 + lev) * 32 + j];
                     __syncwarp();
-                    Real* t = src;
-                    src     = dst;
-                    dst     = t;
+                    Real* tmp = src;
+                    src       = dst;
+                    dst       = tmp;
                 }
                 const Real* R = src; // level 0
-                // G[tuv][kl] += sum (-1)^{tau+nu+phi} E^{kl}_{tau nu phi} R_{t+tau,u+nu,v+phi}
+                // G[tuv][kl] (+)= sum (-1)^{tau+nu+phi} E^{kl}_{tau nu phi} R_{t+tau,u+nu,v+phi}; entries are
+                // lane-owned, restarted at the first ket primitive of every bra primitive.
                 for (int e = lane; e < W::kG; e += 32)
                 {
                     const int h = e / NCD, kl = e % NCD;
                     const int tuv = tabs->htuv[LAB][h];
-                    const int t = tuv & 255, u = (tuv >> 8) & 255, vv = tuv >> 16;
+                    const int tt = tuv & 255, u = (tuv >> 8) & 255, vv = tuv >> 16;
                     const int4 el = tabs->e3[PCK][kl];
                     Real s = Real(0);
                     int x  = el.w;
@@ -219,32 +247,37 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
                         for (int nu = 0; nu < el.y; ++nu)
                             for (int tau = 0; tau < el.x; ++tau, ++x)
                             {
-                                const Real term = rk[x] * R[tabs->cube[L][((t + tau) * S + (u + nu)) * S + (vv + phi)]];
-                                s += ((tau + nu + phi) & 1) ? -term : term;
+                                // The sign rides on the coefficient, so the term is one FMA.
+                                const Real ek = ((tau + nu + phi) & 1) ? -rk[x] : rk[x];
+                                s = fma(ek, R[tabs->cube[L][((tt + tau) * S + (u + nu)) * S + (vv + phi)]], s);
                             }
-                    Gs[e] += s;
+                    Gs[e] = (ik == 0 ? Real(0) : Gs[e]) + s;
                 }
                 __syncwarp();
-            }
-            // ERI[ij][kl] += sum_tuv E^{ij}_{tuv} G[tuv][kl]
-#pragma unroll
-            for (int m = 0; m < W::kAcc; ++m)
-            {
-                const int e = lane + 32 * m;
-                if (e < NAB * NCD)
+                if (ik == npk - 1)
                 {
-                    const int ij = e / NCD, kl = e % NCD;
-                    const int4 el = tabs->e3[PCB][ij];
-                    Real s = Real(0);
-                    int x  = el.w;
-                    for (int vv = 0; vv < el.z; ++vv)
-                        for (int u = 0; u < el.y; ++u)
-                            for (int t = 0; t < el.x; ++t, ++x)
-                                s += rb[x] * Gs[tabs->cube[LAB][(t * (LAB + 1) + u) * (LAB + 1) + vv] * NCD + kl];
-                    acc[m] += s;
+                    // ERI[ij][kl] += sum_tuv E^{ij}_{tuv} G[tuv][kl] for bra primitive ib.
+                    const Real* __restrict__ rb = tb + static_cast<size_t>(bra.pp_off + ib) * SB;
+#pragma unroll
+                    for (int m = 0; m < W::kAcc; ++m)
+                    {
+                        const int e = lane + 32 * m;
+                        if (e < NAB * NCD)
+                        {
+                            const int ij = e / NCD, kl = e % NCD;
+                            const int4 el = tabs->e3[PCB][ij];
+                            Real s = Real(0);
+                            int x  = el.w;
+                            for (int vv = 0; vv < el.z; ++vv)
+                                for (int u = 0; u < el.y; ++u)
+                                    for (int tt = 0; tt < el.x; ++tt, ++x)
+                                        s += rb[x] * Gs[tabs->cube[LAB][(tt * (LAB + 1) + u) * (LAB + 1) + vv] * NCD + kl];
+                            acc[m] += s;
+                        }
+                    }
+                    __syncwarp();
                 }
             }
-            __syncwarp();
         }
 
         if (v.store != nullptr)
