@@ -132,6 +132,15 @@ struct hfg_engine
     // Host records in pack order: pair k's primitives start at record orig_off[k] of h_tab[class].
     std::vector<double> h_tab[hfg::kNumPairClasses];
     std::vector<int> orig_off;
+    // Primitive-pair screening: per record the Coulomb self-repulsion bound sqrt((ab|ab)) of that one
+    // primitive pair; a primitive pair takes part in the Fock build iff bound * max_cd Q_cd >= prim_thr.
+    // Pair k keeps the primitive pairs keep_idx[keep_off[k] .. keep_off[k+1]) of its npp_full[k].
+    double prim_thr = 1e-15;
+    std::vector<double> h_qp[hfg::kNumPairClasses];
+    std::vector<int> npp_full, keep_off, keep_idx;
+    // Unscreened records in pack order (the nuclear gradient's derivative integrals use every primitive).
+    hfg::DevBuf<double> d_pptab64_full[hfg::kNumPairClasses];
+    hfg::DevBuf<hfg::PairRec> d_gspairs; // sorted order, npp_full, pp_off = orig_off
     hfg::DevBuf<long long> d_mat_off;
     hfg::DevBuf<int> d_mat_ld;
     hfg::DevBuf<long long> d_smax_off; // per molecule offset of its shell-max block
@@ -629,16 +638,18 @@ void hermite_1d(int l1, int l2, double p, double PA, double PB, double E[kMaxL +
 }
 } // namespace
 
-// Uploads the pairs and both layouts of the primitive-pair tables for the current pp_off numbering.
+// Uploads the pairs and both layouts of the primitive-pair tables for the current pp_off numbering and
+// the kept primitive pairs of every pair.
 static void upload_pair_tables(hfg_engine* e)
 {
     using namespace hfg;
+    std::vector<size_t> total(kNumPairClasses, 0);
+    for (size_t k = 0; k < e->pairs.size(); ++k) total[e->pair_class_of[k]] += e->pairs[k].npp;
     for (int pc = 0; pc < kNumPairClasses; ++pc)
     {
         const int stride      = pp_stride(pair_class_l1(pc), pair_class_l2(pc));
-        const size_t total    = e->h_tab[pc].size() / stride;
-        const size_t ks       = std::max<size_t>(32, (total + 31) / 32 * 32);
-        std::vector<double> aos(total * stride), soa(ks * stride, 0.0);
+        const size_t ks       = std::max<size_t>(32, (total[pc] + 31) / 32 * 32);
+        std::vector<double> aos(total[pc] * stride), soa(ks * stride, 0.0);
         for (size_t k = 0; k < e->pairs.size(); ++k)
         {
             if (e->pair_class_of[k] != pc)
@@ -646,7 +657,8 @@ static void upload_pair_tables(hfg_engine* e)
             const PairRec& pr = e->pairs[k];
             for (int i = 0; i < pr.npp; ++i)
             {
-                const double* src = &e->h_tab[pc][static_cast<size_t>(e->orig_off[k] + i) * stride];
+                const int idx     = e->keep_idx[e->keep_off[k] + i];
+                const double* src = &e->h_tab[pc][static_cast<size_t>(e->orig_off[k] + idx) * stride];
                 const size_t slot = static_cast<size_t>(pr.pp_off + i);
                 std::copy(src, src + stride, &aos[slot * stride]);
                 const size_t kslot = static_cast<size_t>(pr.kslot) + static_cast<size_t>(i) * pr.kstep;
@@ -660,11 +672,70 @@ static void upload_pair_tables(hfg_engine* e)
         e->kfs[pc] = static_cast<long long>(ks);
     }
     e->d_pairs.upload(e->pairs, e->stream);
-    std::vector<PairRec> sp(e->spair_id.size());
-    for (size_t k = 0; k < sp.size(); ++k) sp[k] = e->pairs[e->spair_id[k]];
+    std::vector<PairRec> sp(e->spair_id.size()), gp(e->spair_id.size());
+    for (size_t k = 0; k < sp.size(); ++k)
+    {
+        const int id = e->spair_id[k];
+        sp[k]        = e->pairs[id];
+        gp[k]        = e->pairs[id];
+        gp[k].npp    = e->npp_full[id];
+        gp[k].pp_off = e->orig_off[id];
+        gp[k].kslot  = e->orig_off[id];
+        gp[k].kstep  = 1;
+    }
     e->d_spairs.upload(sp, e->stream);
+    e->d_gspairs.upload(gp, e->stream);
     HFG_CUDA(cudaStreamSynchronize(e->stream)); // the host vectors above die here
-    e->have_gtab = false;                       // gradient records follow pp_off too
+}
+
+// Coulomb self-repulsion bound sqrt(max_ij (ab_ij|ab_ij)) of ONE primitive pair from its record (p, W,
+// Hermite coefficients E^{ij}_{tuv}).  With P = Q and q = p the Hermite integrals are R_{tuv} =
+// (t-1)!!(u-1)!!(v-1)!! (-p)^n / (2n+1) for even t, u, v (n = (t+u+v)/2) and 0 otherwise, and the
+// prefactor is W^2 / sqrt(2p).  By the Cauchy-Schwarz inequality of the Coulomb metric, the primitive
+// pair's share of any integral (ab|cd) is at most this bound times Q_cd.
+static double prim_self_bound(int l1, int l2, const std::vector<double>& rec)
+{
+    using namespace hfg;
+    const double p = rec[0], W = rec[4];
+    double best    = 0.0;
+    for (int ij = 0; ij < ncart(l1) * ncart(l2); ++ij)
+    {
+        const int lx = e3_len(l1, l2, ij, 0), ly = e3_len(l1, l2, ij, 1), lz = e3_len(l1, l2, ij, 2);
+        const int off = kPairHeader + e3_offset(l1, l2, ij);
+        double acc    = 0.0;
+        for (int e1 = 0; e1 < lx * ly * lz; ++e1)
+            for (int e2 = 0; e2 < lx * ly * lz; ++e2)
+            {
+                const int t = e1 % lx + e2 % lx, u = (e1 / lx) % ly + (e2 / lx) % ly, v = e1 / (lx * ly) + e2 / (lx * ly);
+                if ((t | u | v) & 1)
+                    continue;
+                const int n = (t + u + v) / 2;
+                const int t2 = e2 % lx + (e2 / lx) % ly + e2 / (lx * ly);
+                const double r = dfact_odd(t - 1) * dfact_odd(u - 1) * dfact_odd(v - 1) * std::pow(-p, n) / (2 * n + 1);
+                acc += ((t2 & 1) ? -1.0 : 1.0) * rec[off + e1] * rec[off + e2] * r;
+            }
+        const double an = ang_norm_host(l1, ij / ncart(l2)) * ang_norm_host(l2, ij % ncart(l2));
+        best            = std::max(best, acc * an * an);
+    }
+    return std::sqrt(best) * std::fabs(W) / std::pow(2.0 * p, 0.25);
+}
+
+// Keeps, per pair, the primitive pairs whose bound times max Q reaches prim_thr (all if prim_thr is 0).
+static void screen_primitives(hfg_engine* e)
+{
+    double qmax = 0.0;
+    for (double q : e->Qpair) qmax = std::max(qmax, q);
+    e->keep_off.assign(e->pairs.size() + 1, 0);
+    e->keep_idx.clear();
+    for (size_t k = 0; k < e->pairs.size(); ++k)
+    {
+        const std::vector<double>& qp = e->h_qp[e->pair_class_of[k]];
+        for (int i = 0; i < e->npp_full[k]; ++i)
+            if (!(e->prim_thr > 0.0) || qp[e->orig_off[k] + i] * qmax >= e->prim_thr)
+                e->keep_idx.push_back(i);
+        e->keep_off[k + 1] = static_cast<int>(e->keep_idx.size());
+        e->pairs[k].npp    = e->keep_off[k + 1] - e->keep_off[k];
+    }
 }
 
 // Builds pairs, primitive-pair tables and sorted class lists skeleton (without Q).
@@ -736,14 +807,27 @@ static void pack_molecules(hfg_engine* e)
                                         rec[x++] = E[0][ix][jx][t] * E[1][iy][jy][u] * E[2][iz][jz][v];
                         }
                         tab[pc].insert(tab[pc].end(), rec.begin(), rec.end());
+                        e->h_qp[pc].push_back(prim_self_bound(l1, l2, rec));
                     }
                 class_npp[pc] += pr.npp;
                 e->orig_off.push_back(pr.pp_off);
+                e->npp_full.push_back(pr.npp);
                 e->pairs.push_back(pr);
                 e->pair_class_of.push_back(pc);
             }
     }
-    for (int pc = 0; pc < kNumPairClasses; ++pc) e->h_tab[pc] = std::move(tab[pc]);
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        e->h_tab[pc] = std::move(tab[pc]);
+        e->d_pptab64_full[pc].upload(e->h_tab[pc], e->stream);
+    }
+    e->keep_off.assign(e->pairs.size() + 1, 0);
+    e->keep_idx.clear();
+    for (size_t k = 0; k < e->pairs.size(); ++k)
+    {
+        for (int i = 0; i < e->npp_full[k]; ++i) e->keep_idx.push_back(i);
+        e->keep_off[k + 1] = static_cast<int>(e->keep_idx.size());
+    }
     upload_pair_tables(e);
     std::vector<long long> moff;
     std::vector<int> mld;
@@ -858,6 +942,7 @@ static void compute_schwartz(hfg_engine* e)
 // segments of equal primitive-pair count; uploads the class lists.
 static void sort_classes(hfg_engine* e)
 {
+    screen_primitives(e);
     for (int pc = 0; pc < kNumPairClasses; ++pc)
     {
         auto& ids = e->cls_ids[pc];
@@ -1318,8 +1403,9 @@ static void build_grad_tables(hfg_engine* e)
         const HostBasis& b = e->basis[pr.mol];
         const int l1 = b.l[pr.sh1], l2 = b.l[pr.sh2];
         const int stride = g_stride(l1, l2), n1 = g1d_size(l1, l2);
-        if (tab[pc].size() < static_cast<size_t>(pr.pp_off + pr.npp) * stride)
-            tab[pc].resize(static_cast<size_t>(pr.pp_off + pr.npp) * stride, 0.0);
+        const int pp_off = e->orig_off[k]; // unscreened pack-order layout
+        if (tab[pc].size() < static_cast<size_t>(pp_off + e->npp_full[k]) * stride)
+            tab[pc].resize(static_cast<size_t>(pp_off + e->npp_full[k]) * stride, 0.0);
         const double* A = &b.centers[3 * pr.sh1];
         const double* B = &b.centers[3 * pr.sh2];
         int idx = 0;
@@ -1328,7 +1414,7 @@ static void build_grad_tables(hfg_engine* e)
             {
                 const double aa = b.alpha[b.prim_off[pr.sh1] + pa], ab = b.alpha[b.prim_off[pr.sh2] + pb];
                 const double p = aa + ab, ip = 1.0 / p, h = 0.5 * ip;
-                double* rec = &tab[pc][static_cast<size_t>(pr.pp_off + idx) * stride];
+                double* rec = &tab[pc][static_cast<size_t>(pp_off + idx) * stride];
                 rec[0] = aa;
                 rec[1] = ab;
                 for (int ax = 0; ax < 3; ++ax)
@@ -1378,10 +1464,10 @@ static double gradient_two_electron(hfg_engine* e, const std::vector<int>& shell
     size_lists(e, sthr, false);
     build_lists(e, uhf, false, sthr, dthr, 0.0);
     GradView v {};
-    v.pairs = e->d_spairs.p;
+    v.pairs = e->d_gspairs.p;
     for (int pc = 0; pc < kNumPairClasses; ++pc)
     {
-        v.pptab[pc] = e->d_pptab64[pc].p;
+        v.pptab[pc] = e->d_pptab64_full[pc].p;
         v.gtab[pc]  = e->d_gtab[pc].p;
     }
     v.Dt = e->d_dD[0].p;
@@ -1631,6 +1717,23 @@ int hfg_schwartz(hfg_engine* e, double* Q)
             Q[qoff[p.mol] + p.sh1 + static_cast<long long>(p.sh2) * ns] = e->Qpair[k];
             Q[qoff[p.mol] + p.sh2 + static_cast<long long>(p.sh1) * ns] = e->Qpair[k];
         }
+    });
+}
+
+int hfg_set_primitive_threshold(hfg_engine* e, double threshold)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    if (!(threshold >= 0.0) || !std::isfinite(threshold))
+    {
+        e->last_error = "set_primitive_threshold: threshold must be finite and >= 0";
+        return HFG_ERR_INVALID;
+    }
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        e->prim_thr = threshold;
+        if (e->have_Q)
+            hfg::sort_classes(e); // re-screens, re-sorts and re-uploads the tables
     });
 }
 

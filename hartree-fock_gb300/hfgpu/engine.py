@@ -102,6 +102,7 @@ def lib():
         L.hfg_survivors.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
         L.hfg_eri_block.argtypes = [vp, ip, ip, ip, ip, ctypes.POINTER(ctypes.c_double)]
         L.hfg_set_kernel_form.argtypes = [vp, ip, ip, ip]
+        L.hfg_set_primitive_threshold.argtypes = [vp, ctypes.c_double]
         L.hfg_kernel_forms.argtypes = [vp, ip, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)]
         L.hfg_stream.argtypes = [vp]
         L.hfg_stream.restype = vp
@@ -221,6 +222,10 @@ class Engine:
         st = Stats()
         self._check(lib().hfg_fock_direct(self.h, ctypes.byref(req), ctypes.byref(st)))
         return st.as_dict()
+
+    def set_primitive_threshold(self, threshold: float):
+        """Primitive-pair screening of the Fock build (0 keeps every primitive pair; default 1e-15)."""
+        self._check(lib().hfg_set_primitive_threshold(self.h, float(threshold)))
 
     def set_kernel_form(self, form, qclass=-1, fp32=False):
         """Force a kernel form (FORM_THREAD / FORM_WARP / FORM_GROUP) or return to FORM_AUTO."""

@@ -118,6 +118,14 @@ int hfg_schwartz(hfg_engine* engine, double* Q);
  * own Q so that quartet survival can be compared bit for bit. */
 int hfg_set_schwartz(hfg_engine* engine, const double* Q);
 
+/* Primitive-pair screening of the Fock build (no reference counterpart: the reference evaluates every
+ * primitive pair of a surviving quartet, src/IntegralEngine.cpp:371-520).  A primitive pair ab enters
+ * the build iff sqrt((ab|ab)) * max_cd Q_cd >= threshold, where (ab|ab) is that primitive pair's own
+ * Coulomb self-repulsion: by the Cauchy-Schwarz inequality every dropped term of an integral is below
+ * the threshold.  Default 1e-15; 0 keeps every primitive pair.  Schwartz bounds and the nuclear
+ * gradient always use every primitive pair. */
+int hfg_set_primitive_threshold(hfg_engine* engine, double threshold);
+
 /* SCF::buildFockMatrixDirect (include/SCF.hpp:129, src/SCF.cpp:523-744); `stats` may be NULL. */
 int hfg_fock_direct(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_stats* stats);
 
