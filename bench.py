@@ -255,7 +255,7 @@ def gpu_arm(args, dist):
     import numpy as np
     import torch
 
-    from hfgpu.engine import FP64, MIXED, Engine, measure_fma_peak
+    from hfgpu.engine import FP64, MIXED, Engine, measure_dmma_peak, measure_fma_peak
 
     dev = dist.local
     torch.cuda.set_device(dev)
@@ -328,6 +328,7 @@ def gpu_arm(args, dist):
 
     peak64 = measure_fma_peak(True, dev)
     peak32 = measure_fma_peak(False, dev)
+    peak_dmma = measure_dmma_peak(dev)
     ach64 = st["flops_fp64"] / (st["ms_eri_fp64"] * 1e-3) / 1e12 if st["ms_eri_fp64"] > 0 else 0.0
     ach32 = st["flops_fp32"] / (st["ms_eri_fp32"] * 1e-3) / 1e12 if st["ms_eri_fp32"] > 0 else 0.0
 
@@ -363,7 +364,8 @@ def gpu_arm(args, dist):
                          "peak_source": "measured FP64 FMA loop (hfg_measure_fma_peak) on this GPU",
                          "traffic": None,
                          "fp32_kernels": {"achieved": ach32, "peak": peak32,
-                                          "frac": ach32 / peak32 if peak32 else None}},
+                                          "frac": ach32 / peak32 if peak32 else None},
+                         "fp64_tensor_dmma_tflops": peak_dmma},
             "e2e": {"value": e2e_value, "unit": "Fock builds/s", "h2d_bytes_per_step": 2 * n * n * 8,
                     "d2h_bytes_per_step": 2 * n * n * 8},
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),

@@ -251,10 +251,69 @@ template <typename Real> __device__ __forceinline__ Real ldD(const void* p, long
     return static_cast<const Real*>(p)[i];
 }
 
-// Digestion of one evaluated quartet into X, Ya (, Yb).
+// Density values one quartet's digestion reads: dD_tot over (cd) and (ab); per spin, the exchange
+// partners (bd), (bc), (ad), (ac).
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF> struct DigestD
+{
+    static constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    static constexpr int NS = UHF ? 2 : 1;
+    static constexpr int kCount = NA * NB + NC * ND + NS * (NB * ND + NB * NC + NA * ND + NA * NC);
+    // FP32 kernels (memory-latency bound) load them before the primitive loop, so the loads overlap the
+    // integral evaluation, when they fit in about 40 registers; FP64 kernels (FP64-pipe bound) right
+    // before the digestion.
+    static constexpr bool kEarly = sizeof(Real) == 4 && kCount <= 40;
+    Real Dcd[NC * ND], Dab[NA * NB];
+    Real Dbd[NS][NB * ND], Dbc[NS][NB * NC], Dad[NS][NA * ND], Dac[NS][NA * NC];
+};
+
 template <int LA, int LB, int LC, int LD, typename Real, bool UHF>
-__device__ __forceinline__ void digest_quartet(const PairRec& bra, const PairRec& ket, bool same_pair, const Real* acc,
-                                               const FockView& v)
+__device__ __forceinline__ void load_digest_d(const PairRec& bra, const PairRec& ket, const FockView& v,
+                                              DigestD<LA, LB, LC, LD, Real, UHF>& d)
+{
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    const long long off = v.mat_off[bra.mol];
+    const int n         = v.mat_ld[bra.mol];
+    const int a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
+    auto at = [&](int r, int c) -> long long { return off + r + static_cast<long long>(c) * n; };
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+        for (int l = 0; l < ND; ++l) d.Dcd[k * ND + l] = ldD<Real>(v.Dt, at(c0 + k, d0 + l));
+#pragma unroll
+    for (int i = 0; i < NA; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j) d.Dab[i * NB + j] = ldD<Real>(v.Dt, at(a0 + i, b0 + j));
+#pragma unroll
+    for (int spin = 0; spin < (UHF ? 2 : 1); ++spin)
+    {
+        const void* Ds = spin == 0 ? v.Da : v.Db;
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+        {
+#pragma unroll
+            for (int l = 0; l < ND; ++l) d.Dbd[spin][j * ND + l] = ldD<Real>(Ds, at(b0 + j, d0 + l));
+#pragma unroll
+            for (int k = 0; k < NC; ++k) d.Dbc[spin][j * NC + k] = ldD<Real>(Ds, at(b0 + j, c0 + k));
+        }
+#pragma unroll
+        for (int i = 0; i < NA; ++i)
+        {
+#pragma unroll
+            for (int l = 0; l < ND; ++l) d.Dad[spin][i * ND + l] = ldD<Real>(Ds, at(a0 + i, d0 + l));
+#pragma unroll
+            for (int k = 0; k < NC; ++k) d.Dac[spin][i * NC + k] = ldD<Real>(Ds, at(a0 + i, c0 + k));
+        }
+    }
+}
+
+// Digestion of one evaluated quartet into X, Ya (, Yb), with its density values already loaded.
+// bra_warp: every lane of the warp calls this together and all active lanes hold the same bra pair;
+// the bra's Coulomb block X_ab is then summed over the warp and added once (inactive lanes pass
+// active = false and acc = 0).  Otherwise each active lane adds its own.
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF>
+__device__ __forceinline__ void digest_loaded(const PairRec& bra, const PairRec& ket, bool same_pair, const Real* acc,
+                                              const FockView& v, const DigestD<LA, LB, LC, LD, Real, UHF>& d,
+                                              bool active, bool bra_warp)
 {
     constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
     constexpr int NAB = NA * NB, NCD = NC * ND;
@@ -264,16 +323,6 @@ __device__ __forceinline__ void digest_quartet(const PairRec& bra, const PairRec
     const Real thr = ao_threshold<Real>(v);
     const int a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
     auto at = [&](int r, int c) -> long long { return off + r + static_cast<long long>(c) * n; };
-
-    Real Dcd[NCD], Dab[NAB];
-#pragma unroll
-    for (int k = 0; k < NC; ++k)
-#pragma unroll
-        for (int l = 0; l < ND; ++l) Dcd[k * ND + l] = ldD<Real>(v.Dt, at(c0 + k, d0 + l));
-#pragma unroll
-    for (int i = 0; i < NA; ++i)
-#pragma unroll
-        for (int j = 0; j < NB; ++j) Dab[i * NB + j] = ldD<Real>(v.Dt, at(a0 + i, b0 + j));
 
     Real Jab[NAB], Jcd[NCD];
 #pragma unroll
@@ -285,24 +334,6 @@ __device__ __forceinline__ void digest_quartet(const PairRec& bra, const PairRec
 #pragma unroll
     for (int spin = 0; spin < nspin; ++spin)
     {
-        const void* Ds = spin == 0 ? v.Da : v.Db;
-        Real Dbd[NB * ND], Dbc[NB * NC], Dad[NA * ND], Dac[NA * NC];
-#pragma unroll
-        for (int j = 0; j < NB; ++j)
-        {
-#pragma unroll
-            for (int l = 0; l < ND; ++l) Dbd[j * ND + l] = ldD<Real>(Ds, at(b0 + j, d0 + l));
-#pragma unroll
-            for (int k = 0; k < NC; ++k) Dbc[j * NC + k] = ldD<Real>(Ds, at(b0 + j, c0 + k));
-        }
-#pragma unroll
-        for (int i = 0; i < NA; ++i)
-        {
-#pragma unroll
-            for (int l = 0; l < ND; ++l) Dad[i * ND + l] = ldD<Real>(Ds, at(a0 + i, d0 + l));
-#pragma unroll
-            for (int k = 0; k < NC; ++k) Dac[i * NC + k] = ldD<Real>(Ds, at(a0 + i, c0 + k));
-        }
         Real Kac[NA * NC], Kad[NA * ND], Kbc[NB * NC], Kbd[NB * ND];
 #pragma unroll
         for (int x = 0; x < NA * NC; ++x) Kac[x] = Real(0);
@@ -335,43 +366,76 @@ __device__ __forceinline__ void digest_quartet(const PairRec& bra, const PairRec
                                         const Real w   = (fabs(eri) < thr) ? Real(0) : s * eri;
                                         if (spin == 0)
                                         {
-                                            Jab[i * NB + j] += w * Dcd[k * ND + l];
-                                            Jcd[k * ND + l] += w * Dab[i * NB + j];
+                                            Jab[i * NB + j] += w * d.Dcd[k * ND + l];
+                                            Jcd[k * ND + l] += w * d.Dab[i * NB + j];
                                         }
-                                        Kac[i * NC + k] += w * Dbd[j * ND + l];
-                                        Kad[i * ND + l] += w * Dbc[j * NC + k];
-                                        Kbc[j * NC + k] += w * Dad[i * ND + l];
-                                        Kbd[j * ND + l] += w * Dac[i * NC + k];
+                                        Kac[i * NC + k] += w * d.Dbd[spin][j * ND + l];
+                                        Kad[i * ND + l] += w * d.Dbc[spin][j * NC + k];
+                                        Kbc[j * NC + k] += w * d.Dad[spin][i * ND + l];
+                                        Kbd[j * ND + l] += w * d.Dac[spin][i * NC + k];
                                     });
                             });
                     });
             });
-        double* Y = spin == 0 ? v.Ya : v.Yb;
-#pragma unroll
-        for (int i = 0; i < NA; ++i)
+        if (active)
         {
+            double* Y = spin == 0 ? v.Ya : v.Yb;
 #pragma unroll
-            for (int k = 0; k < NC; ++k) atomicAdd(Y + at(a0 + i, c0 + k), double(Kac[i * NC + k]));
+            for (int i = 0; i < NA; ++i)
+            {
 #pragma unroll
-            for (int l = 0; l < ND; ++l) atomicAdd(Y + at(a0 + i, d0 + l), double(Kad[i * ND + l]));
-        }
+                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(a0 + i, c0 + k), double(Kac[i * NC + k]));
 #pragma unroll
-        for (int j = 0; j < NB; ++j)
-        {
+                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(a0 + i, d0 + l), double(Kad[i * ND + l]));
+            }
 #pragma unroll
-            for (int k = 0; k < NC; ++k) atomicAdd(Y + at(b0 + j, c0 + k), double(Kbc[j * NC + k]));
+            for (int j = 0; j < NB; ++j)
+            {
 #pragma unroll
-            for (int l = 0; l < ND; ++l) atomicAdd(Y + at(b0 + j, d0 + l), double(Kbd[j * ND + l]));
+                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(b0 + j, c0 + k), double(Kbc[j * NC + k]));
+#pragma unroll
+                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(b0 + j, d0 + l), double(Kbd[j * ND + l]));
+            }
         }
     }
+    if (bra_warp)
+    {
+        // Warp sum of the bra block, in double, then one atomic per element from lane 0.
+        const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int i = 0; i < NA; ++i)
+        for (int x = 0; x < NAB; ++x)
+        {
+            double t = double(Jab[x]);
 #pragma unroll
-        for (int j = 0; j < NB; ++j) atomicAdd(v.X + at(a0 + i, b0 + j), 2.0 * double(Jab[i * NB + j]));
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0)
+                atomicAdd(v.X + at(a0 + x / NB, b0 + x % NB), 2.0 * t);
+        }
+    }
+    else if (active)
+    {
 #pragma unroll
-    for (int k = 0; k < NC; ++k)
+        for (int i = 0; i < NA; ++i)
 #pragma unroll
-        for (int l = 0; l < ND; ++l) atomicAdd(v.X + at(c0 + k, d0 + l), 2.0 * double(Jcd[k * ND + l]));
+            for (int j = 0; j < NB; ++j) atomicAdd(v.X + at(a0 + i, b0 + j), 2.0 * double(Jab[i * NB + j]));
+    }
+    if (active)
+    {
+#pragma unroll
+        for (int k = 0; k < NC; ++k)
+#pragma unroll
+            for (int l = 0; l < ND; ++l) atomicAdd(v.X + at(c0 + k, d0 + l), 2.0 * double(Jcd[k * ND + l]));
+    }
+}
+
+// Digestion of one evaluated quartet by one lane on its own.
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF>
+__device__ __forceinline__ void digest_quartet(const PairRec& bra, const PairRec& ket, bool same_pair, const Real* acc,
+                                               const FockView& v)
+{
+    DigestD<LA, LB, LC, LD, Real, UHF> d;
+    load_digest_d<LA, LB, LC, LD, Real, UHF>(bra, ket, v, d);
+    digest_loaded<LA, LB, LC, LD, Real, UHF>(bra, ket, same_pair, acc, v, d, true, false);
 }
 
 // Stage this class's Boys slice in shared memory.
@@ -399,28 +463,48 @@ __global__ void __launch_bounds__(128) jk_class_kernel(const Quartet* __restrict
     const Real* tb      = static_cast<const Real*>(v.pptab[pair_class(LA, LB)]);
     const Real* tk      = static_cast<const Real*>(v.ksoa[pair_class(LC, LD)]);
     const long long kfs = v.kfs[pair_class(LC, LD)];
-    for (unsigned long long q = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
-         q += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+    using DD   = DigestD<LA, LB, LC, LD, Real, UHF>;
+    const int lane = threadIdx.x & 31;
+    // Warp-uniform iteration (every lane runs the same trip count, inactive lanes past the end), so that
+    // the digestion may sum the bra block over the warp.
+    for (unsigned long long base = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u);
+         base < n; base += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
     {
-        const Quartet qt  = list[q];
-        const PairRec bra = v.pairs[qt.bra];
-        const PairRec ket = v.pairs[qt.ket];
+        const unsigned long long q = base + lane;
+        const bool active          = q < n;
+        const Quartet qt           = list[active ? q : base];
+        const PairRec bra          = v.pairs[qt.bra];
+        const PairRec ket          = v.pairs[qt.ket];
+        DD d;
+        if (v.store == nullptr && DD::kEarly)
+            load_digest_d<LA, LB, LC, LD, Real, UHF>(bra, ket, v, d);
         Real acc[N];
-        eval_quartet<LA, LB, LC, LD, Real, true>(bra, ket, tb, tk, slice, acc, kfs);
+        if (active)
+            eval_quartet<LA, LB, LC, LD, Real, true>(bra, ket, tb, tk, slice, acc, kfs);
+        else
+        {
+#pragma unroll
+            for (int x = 0; x < N; ++x) acc[x] = Real(0);
+        }
         if (v.store != nullptr)
         {
-            static_for<0, N>(
-                [&](auto E)
-                {
-                    constexpr int e  = decltype(E)::value;
-                    constexpr int NB = ncart(LB), NC = ncart(LC), ND = ncart(LD), NCD = NC * ND;
-                    constexpr double an = ang_norm(LA, e / NCD / NB) * ang_norm(LB, (e / NCD) % NB)
-                                        * ang_norm(LC, (e % NCD) / ND) * ang_norm(LD, e % ND);
-                    v.store[q * N + e] = double(acc[e]) * an;
-                });
+            if (active)
+                static_for<0, N>(
+                    [&](auto E)
+                    {
+                        constexpr int e  = decltype(E)::value;
+                        constexpr int NB = ncart(LB), NC = ncart(LC), ND = ncart(LD), NCD = NC * ND;
+                        constexpr double an = ang_norm(LA, e / NCD / NB) * ang_norm(LB, (e / NCD) % NB)
+                                            * ang_norm(LC, (e % NCD) / ND) * ang_norm(LD, e % ND);
+                        v.store[q * N + e] = double(acc[e]) * an;
+                    });
             continue;
         }
-        digest_quartet<LA, LB, LC, LD, Real, UHF>(bra, ket, qt.bra == qt.ket, acc, v);
+        if (!DD::kEarly)
+            load_digest_d<LA, LB, LC, LD, Real, UHF>(bra, ket, v, d);
+        const unsigned bra0 = __shfl_sync(0xffffffffu, qt.bra, 0);
+        const bool bra_warp = __all_sync(0xffffffffu, qt.bra == bra0);
+        digest_loaded<LA, LB, LC, LD, Real, UHF>(bra, ket, qt.bra == qt.ket, acc, v, d, active, bra_warp);
     }
 }
 

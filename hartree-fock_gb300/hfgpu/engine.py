@@ -116,6 +116,7 @@ def lib():
         L.hfg_core_guess.argtypes = [vp, ctypes.POINTER(ScfOptions), ip, ctypes.POINTER(ctypes.c_int), dpp, ip, ip,
                                      dpp, dpp]
         L.hfg_measure_fma_peak.argtypes = [ip, ip, dpp]
+        L.hfg_measure_dmma_peak.argtypes = [ip, dpp]
         L.hfg_gradient.argtypes = [vp, ctypes.POINTER(GradRequest), dpp, dpp]
         _lib = L
     return _lib
@@ -317,6 +318,15 @@ def measure_fma_peak(fp64: bool, device: int = 0) -> float:
     rc = lib().hfg_measure_fma_peak(device, 1 if fp64 else 0, ctypes.byref(t))
     if rc != HFG_OK:
         raise HfgError(rc, "hfg_measure_fma_peak failed")
+    return t.value
+
+
+def measure_dmma_peak(device: int = 0) -> float:
+    """TFLOP/s of a register-only FP64 tensor-core (DMMA m8n8k4) loop on this GPU."""
+    t = ctypes.c_double()
+    rc = lib().hfg_measure_dmma_peak(device, ctypes.byref(t))
+    if rc != HFG_OK:
+        raise HfgError(rc, "hfg_measure_dmma_peak failed")
     return t.value
 
 

@@ -261,6 +261,8 @@ int hfg_gradient_one_electron(const hfg_basis* basis, const int* shell_atom, int
 /* Peak FMA throughput of this GPU measured by a register-only FMA loop (TFLOP/s, FP64 if fp64 != 0,
  * else FP32): the denominator of the ERI kernels' roofline. */
 int hfg_measure_fma_peak(int device, int fp64, double* tflops);
+/* FP64 tensor-core (DMMA m8n8k4) throughput of this GPU in TFLOP/s (no reference counterpart). */
+int hfg_measure_dmma_peak(int device, double* tflops);
 
 /* Library version string. */
 const char* hfg_version(void);
