@@ -203,6 +203,26 @@ struct hfg_engine
     hfg::DevBuf<double> d_tune_acc[3];
     cudaEvent_t tune_ev[2] {};
 
+    // CUDA-graph replay of whole builds (hfg_set_graph_mode): the graph of the last device-pointer
+    // request, valid while the request key matches and no buffer it uses has been reallocated.
+    bool graph_mode = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    struct GraphKey
+    {
+        int precision = -1, uhf = 0;
+        double sthr = 0, dthr = 0, cutoff = 0;
+        const void* ptr[6] {};
+        bool operator==(const GraphKey& o) const
+        {
+            return precision == o.precision && uhf == o.uhf && sthr == o.sthr && dthr == o.dthr && cutoff == o.cutoff &&
+                   std::equal(ptr, ptr + 6, o.ptr);
+        }
+    } graph_key;
+    int graph_launches = 0;
+    int graph_forms[hfg::kNumQuartetClasses][2] {};
+    unsigned long long* h_counts_pin = nullptr; // pinned copy of d_counts written by the graph
+
     bool last_valid = false;
     int last_mixed  = 0;
 };
@@ -638,11 +658,23 @@ void hermite_1d(int l1, int l2, double p, double PA, double PB, double E[kMaxL +
 }
 } // namespace
 
+// Drops the captured build graph (a buffer it uses is about to change).
+static void invalidate_graph(hfg_engine* e)
+{
+    if (e->graph_exec)
+        cudaGraphExecDestroy(e->graph_exec);
+    if (e->graph)
+        cudaGraphDestroy(e->graph);
+    e->graph_exec = nullptr;
+    e->graph      = nullptr;
+}
+
 // Uploads the pairs and both layouts of the primitive-pair tables for the current pp_off numbering and
 // the kept primitive pairs of every pair.
 static void upload_pair_tables(hfg_engine* e)
 {
     using namespace hfg;
+    invalidate_graph(e);
     std::vector<size_t> total(kNumPairClasses, 0);
     for (size_t k = 0; k < e->pairs.size(); ++k) total[e->pair_class_of[k]] += e->pairs[k].npp;
     for (int pc = 0; pc < kNumPairClasses; ++pc)
@@ -1040,6 +1072,7 @@ static void size_lists(hfg_engine* e, double sthr, bool mixed)
 {
     if (e->cap_thr == sthr && (!mixed || e->cap_mixed))
         return;
+    invalidate_graph(e);
     for (int P1 = 0; P1 < kNumPairClasses; ++P1)
         for (int P2 = 0; P2 <= P1; ++P2)
         {
@@ -1068,7 +1101,8 @@ static void size_lists(hfg_engine* e, double sthr, bool mixed)
 
 // Screening and the survival lists of every quartet class from the densities already in d_dD[0..2]
 // (the shell-pair maxima, then count pass, scan and write pass per class).  Returns the launches.
-static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double dthr, double cutoff)
+// graph: enqueue only (no host synchronisation); the counts go to the pinned buffer, checked after replay.
+static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double dthr, double cutoff, bool graph = false)
 {
     cudaStream_t s  = e->stream;
     const int nspin = uhf ? 3 : 2;
@@ -1150,6 +1184,8 @@ static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double 
                     launches += 3;
                 }
             }
+    if (graph)
+        return launches + nspin;
     e->h_counts.assign(2 * ncnt + 1, 0);
     HFG_CUDA(cudaMemcpyAsync(e->h_counts.data(), e->d_counts.p, sizeof(unsigned long long) * (2 * ncnt + 1),
                              cudaMemcpyDeviceToHost, s));
@@ -1239,37 +1275,21 @@ int pick_form(hfg_engine* e, int qc, int prec, bool uhf, const ClassLaunch& base
     return pick;
 }
 
-static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats* st)
+// Enqueues one build on the engine stream.  Eager (graph == false): timing events, list lengths read
+// back after the list build, only non-empty classes launched, forms tuned on first use.  Graph: nothing
+// that needs the host (no read-back, no tuning): every class with a non-empty capacity is launched
+// with the grid of its capacity (the kernels read their list lengths on the device, so surplus blocks
+// exit at once), and the counts are copied to pinned memory for the host to read after the replay.
+static int enqueue_build(hfg_engine* e, const hfg_fock_request& r, bool graph, int form_ran[][2], double* ms_tune)
 {
-    if (!(r.schwartz_threshold >= 0.0) || !(r.density_threshold >= 0.0) || !std::isfinite(r.schwartz_threshold) ||
-        !std::isfinite(r.density_threshold))
-        throw HfgError(HFG_ERR_INVALID, "fock: thresholds must be finite and >= 0");
-    if (!r.dD_tot || !r.dD_alpha || !r.J || !r.K_alpha || (r.unrestricted && (!r.dD_beta || !r.K_beta)))
-        throw HfgError(HFG_ERR_INVALID, "fock: missing matrix pointer");
-    if (r.precision != HFG_PRECISION_FP64 && r.precision != HFG_PRECISION_MIXED)
-        throw HfgError(HFG_ERR_INVALID, "fock: unknown precision mode");
-    const bool mixed = r.precision == HFG_PRECISION_MIXED;
-    const bool uhf   = r.unrestricted != 0;
-    if (!e->have_Q)
-    {
-        compute_schwartz(e);
-        sort_classes(e);
-    }
-    size_lists(e, r.schwartz_threshold, mixed);
+    const bool mixed   = r.precision == HFG_PRECISION_MIXED;
+    const bool uhf     = r.unrestricted != 0;
     const long long N2 = e->mat_total;
     cudaStream_t s     = e->stream;
     const int nspin    = uhf ? 3 : 2;
     const double* src[3] = {r.dD_tot, r.dD_alpha, r.dD_beta};
-    for (int k = 0; k < 3; ++k)
-    {
-        e->d_dD[k].alloc(N2);
-        e->d_acc[k].alloc(N2);
-        e->d_out[k].alloc(N2);
-        e->d_smax[k].alloc(e->smax_total);
-        if (mixed)
-            e->d_dDf[k].alloc(N2);
-    }
-    HFG_CUDA(cudaEventRecord(e->ev[0], s));
+    if (!graph)
+        HFG_CUDA(cudaEventRecord(e->ev[0], s));
     for (int k = 0; k < nspin; ++k)
     {
         HFG_CUDA(cudaMemcpyAsync(e->d_dD[k].p, src[k], sizeof(double) * N2,
@@ -1281,20 +1301,20 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
             HFG_CUDA(cudaGetLastError());
         }
     }
-    HFG_CUDA(cudaEventRecord(e->ev[1], s));
+    if (!graph)
+        HFG_CUDA(cudaEventRecord(e->ev[1], s));
 
-    int launches = nspin * (mixed ? 2 : 1) + build_lists(e, uhf, mixed, r.schwartz_threshold, r.density_threshold, r.fp32_cutoff);
-    const int ncnt = kNumQuartetClasses * 2;
-    int form_ran[kNumQuartetClasses][2] {};
-    double ms_tune = 0.0;
+    int launches = nspin * (mixed ? 2 : 1) +
+                   build_lists(e, uhf, mixed, r.schwartz_threshold, r.density_threshold, r.fp32_cutoff, graph);
 
     // Class kernels: FP64 lists, then FP32 lists.
     for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
     {
-        HFG_CUDA(cudaEventRecord(e->ev[3 + prec], s));
+        if (!graph)
+            HFG_CUDA(cudaEventRecord(e->ev[3 + prec], s));
         for (int qc = kNumQuartetClasses - 1; qc >= 0; --qc)
         {
-            const unsigned long long n = e->h_counts[2 * qc + prec];
+            const unsigned long long n = graph ? e->cap[qc] : e->h_counts[2 * qc + prec];
             if (n == 0)
                 continue;
             const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
@@ -1320,13 +1340,21 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
             c.uhf        = uhf;
             c.stream     = s;
             c.num_sms    = e->num_sms;
-            c.form       = pick_form(e, qc, prec, uhf, c, &ms_tune);
+            if (graph)
+            {
+                const int set  = e->form_set[qc][prec];
+                const int pick = e->form_pick[qc][prec][uhf ? 1 : 0];
+                c.form         = set != 0 ? set : pick;
+            }
+            else
+                c.form = pick_form(e, qc, prec, uhf, c, ms_tune);
             HFG_CUDA(launch_class(qc, c));
-            form_ran[qc][prec] = c.form != 0 ? c.form : (class_default_form(qc, prec == 1));
+            form_ran[qc][prec] = c.form != 0 ? c.form : class_default_form(qc, prec == 1);
             ++launches;
         }
     }
-    HFG_CUDA(cudaEventRecord(e->ev[5], s));
+    if (!graph)
+        HFG_CUDA(cudaEventRecord(e->ev[5], s));
     double* outs[3] = {r.J, r.K_alpha, r.K_beta};
     for (int k = 0; k < nspin; ++k)
     {
@@ -1335,27 +1363,114 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
         HFG_CUDA(cudaGetLastError());
         ++launches;
     }
-    HFG_CUDA(cudaEventRecord(e->ev[6], s));
+    if (!graph)
+        HFG_CUDA(cudaEventRecord(e->ev[6], s));
     for (int k = 0; k < nspin; ++k)
         HFG_CUDA(cudaMemcpyAsync(outs[k], e->d_out[k].p, sizeof(double) * N2,
                                  r.device_pointers ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    if (graph)
+        HFG_CUDA(cudaMemcpyAsync(e->h_counts_pin, e->d_counts.p, sizeof(unsigned long long) * (4 * kNumQuartetClasses + 1),
+                                 cudaMemcpyDeviceToHost, s));
+    return launches;
+}
+
+static void fill_stats(hfg_engine* e, bool uhf, int launches, int form_ran[][2], double ms_tune, hfg_fock_stats* st)
+{
+    const int ncnt = kNumQuartetClasses * 2;
+    std::memset(st, 0, sizeof(*st));
+    for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+    {
+        st->quartets_fp64[qc]      = e->h_counts[2 * qc];
+        st->quartets_fp32[qc]      = e->h_counts[2 * qc + 1];
+        st->prim_quartets_fp64[qc] = e->h_counts[ncnt + 2 * qc];
+        st->prim_quartets_fp32[qc] = e->h_counts[ncnt + 2 * qc + 1];
+        st->flops_fp64 += flops_per_prim_quartet(qc) * st->prim_quartets_fp64[qc] +
+                          flops_per_quartet_digest(qc, uhf) * st->quartets_fp64[qc];
+        st->flops_fp32 += flops_per_prim_quartet(qc) * st->prim_quartets_fp32[qc] +
+                          flops_per_quartet_digest(qc, uhf) * st->quartets_fp32[qc];
+        st->form_fp64[qc] = st->quartets_fp64[qc] ? form_ran[qc][0] : 0;
+        st->form_fp32[qc] = st->quartets_fp32[qc] ? form_ran[qc][1] : 0;
+    }
+    st->kernel_launches = launches;
+    st->ms_tune         = ms_tune;
+}
+
+static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats* st)
+{
+    if (!(r.schwartz_threshold >= 0.0) || !(r.density_threshold >= 0.0) || !std::isfinite(r.schwartz_threshold) ||
+        !std::isfinite(r.density_threshold))
+        throw HfgError(HFG_ERR_INVALID, "fock: thresholds must be finite and >= 0");
+    if (!r.dD_tot || !r.dD_alpha || !r.J || !r.K_alpha || (r.unrestricted && (!r.dD_beta || !r.K_beta)))
+        throw HfgError(HFG_ERR_INVALID, "fock: missing matrix pointer");
+    if (r.precision != HFG_PRECISION_FP64 && r.precision != HFG_PRECISION_MIXED)
+        throw HfgError(HFG_ERR_INVALID, "fock: unknown precision mode");
+    const bool mixed = r.precision == HFG_PRECISION_MIXED;
+    const bool uhf   = r.unrestricted != 0;
+    if (!e->have_Q)
+    {
+        compute_schwartz(e);
+        sort_classes(e);
+    }
+    size_lists(e, r.schwartz_threshold, mixed);
+    const long long N2 = e->mat_total;
+    cudaStream_t s     = e->stream;
+    for (int k = 0; k < 3; ++k)
+    {
+        e->d_dD[k].alloc(N2);
+        e->d_acc[k].alloc(N2);
+        e->d_out[k].alloc(N2);
+        e->d_smax[k].alloc(e->smax_total);
+        e->d_smaxf[k].alloc(e->smax_total);
+        if (mixed && !e->d_dDf[k].p)
+        {
+            invalidate_graph(e);
+            e->d_dDf[k].alloc(N2);
+        }
+    }
+    e->d_smax2.alloc(e->smax_total);
+    const int ncnt = kNumQuartetClasses * 2;
+    const bool use_graph = e->graph_mode && r.device_pointers;
+    hfg_engine::GraphKey key;
+    key.precision = r.precision;
+    key.uhf       = uhf ? 1 : 0;
+    key.sthr      = r.schwartz_threshold;
+    key.dthr      = r.density_threshold;
+    key.cutoff    = mixed ? r.fp32_cutoff : 0.0;
+    const void* ptrs[6] = {r.dD_tot, r.dD_alpha, uhf ? r.dD_beta : nullptr, r.J, r.K_alpha, uhf ? r.K_beta : nullptr};
+    std::copy(ptrs, ptrs + 6, key.ptr);
+
+    if (use_graph && e->graph_exec && key == e->graph_key)
+    {
+        // Replay.
+        HFG_CUDA(cudaEventRecord(e->ev[1], s));
+        HFG_CUDA(cudaGraphLaunch(e->graph_exec, s));
+        HFG_CUDA(cudaEventRecord(e->ev[6], s));
+        HFG_CUDA(cudaStreamSynchronize(s));
+        e->h_counts.assign(e->h_counts_pin, e->h_counts_pin + 2 * ncnt + 1);
+        for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+            if (e->h_counts[2 * qc] > e->cap[qc] || e->h_counts[2 * qc + 1] > e->cap[qc])
+                throw HfgError(HFG_ERR_OVERFLOW, "fock: quartet list overflow");
+        e->last_valid = true;
+        e->last_mixed = mixed ? 1 : 0;
+        if (st)
+        {
+            fill_stats(e, uhf, e->graph_launches, e->graph_forms, 0.0, st);
+            float ms = 0.f;
+            HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[1], e->ev[6]));
+            st->ms_total = ms; // the split into lists / FP64 / FP32 is not timed inside a graph
+        }
+        return;
+    }
+
+    int form_ran[kNumQuartetClasses][2] {};
+    double ms_tune = 0.0;
+    const int launches = enqueue_build(e, r, false, form_ran, &ms_tune);
     HFG_CUDA(cudaStreamSynchronize(s));
     e->last_valid = true;
     e->last_mixed = mixed ? 1 : 0;
     if (st)
     {
-        std::memset(st, 0, sizeof(*st));
-        for (int qc = 0; qc < kNumQuartetClasses; ++qc)
-        {
-            st->quartets_fp64[qc]      = e->h_counts[2 * qc];
-            st->quartets_fp32[qc]      = e->h_counts[2 * qc + 1];
-            st->prim_quartets_fp64[qc] = e->h_counts[ncnt + 2 * qc];
-            st->prim_quartets_fp32[qc] = e->h_counts[ncnt + 2 * qc + 1];
-            st->flops_fp64 += flops_per_prim_quartet(qc) * st->prim_quartets_fp64[qc] +
-                              flops_per_quartet_digest(qc, uhf) * st->quartets_fp64[qc];
-            st->flops_fp32 += flops_per_prim_quartet(qc) * st->prim_quartets_fp32[qc] +
-                              flops_per_quartet_digest(qc, uhf) * st->quartets_fp32[qc];
-        }
+        fill_stats(e, uhf, launches, form_ran, ms_tune, st);
         float ms = 0.f;
         HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[1], e->ev[6]));
         st->ms_total = ms;
@@ -1368,13 +1483,34 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
             HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[4], e->ev[5]));
             st->ms_eri_fp32 = ms;
         }
-        st->kernel_launches = launches;
-        for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+    }
+    if (use_graph)
+    {
+        // Capture the same build for the next calls with this key (forms are tuned by now).
+        invalidate_graph(e);
+        if (!e->h_counts_pin)
+            HFG_CUDA(cudaMallocHost(&e->h_counts_pin, sizeof(unsigned long long) * (2 * ncnt + 1)));
+        int forms[kNumQuartetClasses][2] {};
+        double unused = 0.0;
+        HFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+        int glaunches = 0;
+        try
         {
-            st->form_fp64[qc] = form_ran[qc][0];
-            st->form_fp32[qc] = form_ran[qc][1];
+            glaunches = enqueue_build(e, r, true, forms, &unused);
         }
-        st->ms_tune = ms_tune;
+        catch (...)
+        {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(s, &g);
+            if (g)
+                cudaGraphDestroy(g);
+            throw;
+        }
+        HFG_CUDA(cudaStreamEndCapture(s, &e->graph));
+        HFG_CUDA(cudaGraphInstantiate(&e->graph_exec, e->graph, 0));
+        e->graph_key      = key;
+        e->graph_launches = glaunches;
+        std::memcpy(e->graph_forms, forms, sizeof(forms));
     }
 }
 
@@ -1679,7 +1815,13 @@ void hfg_destroy(hfg_engine* e)
     cudaSetDevice(e->device);
     if (e->stream)
         cudaStreamSynchronize(e->stream);
+    hfg::invalidate_graph(e);
+    if (e->h_counts_pin)
+        cudaFreeHost(e->h_counts_pin);
     for (auto& ev : e->ev)
+        if (ev)
+            cudaEventDestroy(ev);
+    for (auto& ev : e->tune_ev)
         if (ev)
             cudaEventDestroy(ev);
     if (e->stream)
@@ -1787,6 +1929,7 @@ int hfg_set_kernel_form(hfg_engine* e, int qclass, int fp32, int form)
         return HFG_ERR_INVALID;
     }
     const int lo = qclass < 0 ? 0 : qclass, hi = qclass < 0 ? hfg::kNumQuartetClasses : qclass + 1;
+    hfg::invalidate_graph(e); // a captured build holds the old forms
     for (int qc = lo; qc < hi; ++qc)
     {
         const bool ok = form == HFG_FORM_AUTO || ((hfg::class_form_mask(qc, fp32 != 0) >> form) & 1u);
@@ -1805,6 +1948,18 @@ int hfg_set_kernel_form(hfg_engine* e, int qclass, int fp32, int form)
             e->form_pick[qc][fp32][0] = e->form_pick[qc][fp32][1] = 0;
     }
     return HFG_OK;
+}
+
+int hfg_set_graph_mode(hfg_engine* e, int on)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        e->graph_mode = on != 0;
+        if (!e->graph_mode)
+            hfg::invalidate_graph(e);
+    });
 }
 
 int hfg_kernel_forms(hfg_engine* e, int fp32, int unrestricted, int* forms, unsigned* available)

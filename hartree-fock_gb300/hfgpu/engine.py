@@ -103,6 +103,7 @@ def lib():
         L.hfg_eri_block.argtypes = [vp, ip, ip, ip, ip, ctypes.POINTER(ctypes.c_double)]
         L.hfg_set_kernel_form.argtypes = [vp, ip, ip, ip]
         L.hfg_set_primitive_threshold.argtypes = [vp, ctypes.c_double]
+        L.hfg_set_graph_mode.argtypes = [vp, ip]
         L.hfg_kernel_forms.argtypes = [vp, ip, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)]
         L.hfg_stream.argtypes = [vp]
         L.hfg_stream.restype = vp
@@ -224,6 +225,10 @@ class Engine:
         self._check(lib().hfg_fock_direct(self.h, ctypes.byref(req), ctypes.byref(st)))
         return st.as_dict()
 
+    def set_graph_mode(self, on: bool):
+        """Replay device-pointer Fock builds as CUDA graphs (captured on first use per request key)."""
+        self._check(lib().hfg_set_graph_mode(self.h, 1 if on else 0))
+
     def set_primitive_threshold(self, threshold: float):
         """Primitive-pair screening of the Fock build (0 keeps every primitive pair; default 1e-15)."""
         self._check(lib().hfg_set_primitive_threshold(self.h, float(threshold)))
@@ -331,13 +336,16 @@ def measure_dmma_peak(device: int = 0) -> float:
 
 
 def run_input(text: str, precision: int = FP64, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0,
-              basis_dir: str | None = None, device: int = 0):
-    """Runs a reference-format input end to end: parse, pack the basis, GPU direct SCF."""
+              basis_dir: str | None = None, device: int = 0, graphs: bool = False):
+    """Runs a reference-format input end to end: parse, pack the basis, GPU direct SCF (graphs: replay
+    the Fock builds of the SCF iterations as CUDA graphs)."""
     from . import basis as _basis, inputs as _inputs
 
     job = _inputs.parse(text)
     soa = _basis.pack(job.basis, job.Z, job.xyz, basis_dir)
     eng = Engine(soa, device=device)
+    if graphs:
+        eng.set_graph_mode(True)
     opts = _inputs.scf_options(job, precision, fp32_cutoff, full_rebuild_every)
     res, Da, Db = eng.scf(job.Z, job.xyz, job.charge, job.multiplicity, opts)
     return res, Da, Db, eng

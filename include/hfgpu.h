@@ -143,6 +143,15 @@ int hfg_fock_direct(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_st
  * kernels).  HFG_FORM_AUTO forgets earlier timings; a form the class was not compiled in returns
  * HFG_ERR_UNSUPPORTED (with qclass -1 such classes keep AUTO). */
 int hfg_set_kernel_form(hfg_engine* engine, int qclass, int fp32, int form);
+/* CUDA-graph replay of Fock builds (no reference counterpart; the SCF driver calls hfg_fock_direct on
+ * device pointers every iteration).  On: a device-pointer request runs eagerly once and is captured
+ * with every class kernel at a fixed grid (the kernels read their list lengths on the device); later
+ * requests with the same precision, spin case, thresholds, cutoff and matrix pointers replay the
+ * graph as one launch.  Changing forms, thresholds or the Schwartz matrix drops the graph.  Replays
+ * report ms_total but not its split into lists / FP64 / FP32.  Off by default; host-pointer requests
+ * always run eagerly. */
+int hfg_set_graph_mode(hfg_engine* engine, int on);
+
 /* Forms in use: forms[qc] for the given precision and spin case, 0 where AUTO has not decided yet.
  * `available` (may be NULL) receives the bit mask of compiled forms per class (bit f = form f). */
 int hfg_kernel_forms(hfg_engine* engine, int fp32, int unrestricted, int forms[HFG_NUM_CLASSES],
