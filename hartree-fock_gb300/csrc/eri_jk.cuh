@@ -238,6 +238,21 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
     }
 }
 
+// Widening to double for the FP64 accumulators without the FP64 pipe (GB300 runs float -> double
+// conversions there, at 1/64 of the FP32 rate): the IEEE-754 fields are moved with integer operations.
+// Exact for normal numbers and zero; float subnormals (< 1.2e-38) become zero; infinities and NaNs keep
+// their class.
+__device__ __forceinline__ double widen(float x)
+{
+    const unsigned u                 = __float_as_uint(x);
+    const unsigned e                 = (u >> 23) & 0xffu;
+    const unsigned long long sign    = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+    const unsigned long long de      = e == 0xffu ? 0x7ffull : static_cast<unsigned long long>(e + 896u);
+    const unsigned long long normal  = sign | (de << 52) | (static_cast<unsigned long long>(u & 0x7fffffu) << 29);
+    return __longlong_as_double(static_cast<long long>(e == 0u ? sign : normal));
+}
+__device__ __forceinline__ double widen(double x) { return x; }
+
 template <typename Real> __device__ __forceinline__ Real ao_threshold(const FockView& v)
 {
     if constexpr (sizeof(Real) == 4)
@@ -384,32 +399,32 @@ __device__ __forceinline__ void digest_loaded(const PairRec& bra, const PairRec&
             for (int i = 0; i < NA; ++i)
             {
 #pragma unroll
-                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(a0 + i, c0 + k), double(Kac[i * NC + k]));
+                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(a0 + i, c0 + k), widen(Kac[i * NC + k]));
 #pragma unroll
-                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(a0 + i, d0 + l), double(Kad[i * ND + l]));
+                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(a0 + i, d0 + l), widen(Kad[i * ND + l]));
             }
 #pragma unroll
             for (int j = 0; j < NB; ++j)
             {
 #pragma unroll
-                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(b0 + j, c0 + k), double(Kbc[j * NC + k]));
+                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(b0 + j, c0 + k), widen(Kbc[j * NC + k]));
 #pragma unroll
-                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(b0 + j, d0 + l), double(Kbd[j * ND + l]));
+                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(b0 + j, d0 + l), widen(Kbd[j * ND + l]));
             }
         }
     }
     if (bra_warp)
     {
-        // Warp sum of the bra block, in double, then one atomic per element from lane 0.
+        // Warp sum of the bra block, then one atomic per element from lane 0.
         const int lane = threadIdx.x & 31;
 #pragma unroll
         for (int x = 0; x < NAB; ++x)
         {
-            double t = double(Jab[x]);
+            Real t = Jab[x];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
             if (lane == 0)
-                atomicAdd(v.X + at(a0 + x / NB, b0 + x % NB), 2.0 * t);
+                atomicAdd(v.X + at(a0 + x / NB, b0 + x % NB), widen(Real(2) * t));
         }
     }
     else if (active)
@@ -417,14 +432,14 @@ __device__ __forceinline__ void digest_loaded(const PairRec& bra, const PairRec&
 #pragma unroll
         for (int i = 0; i < NA; ++i)
 #pragma unroll
-            for (int j = 0; j < NB; ++j) atomicAdd(v.X + at(a0 + i, b0 + j), 2.0 * double(Jab[i * NB + j]));
+            for (int j = 0; j < NB; ++j) atomicAdd(v.X + at(a0 + i, b0 + j), widen(Real(2) * Jab[i * NB + j]));
     }
     if (active)
     {
 #pragma unroll
         for (int k = 0; k < NC; ++k)
 #pragma unroll
-            for (int l = 0; l < ND; ++l) atomicAdd(v.X + at(c0 + k, d0 + l), 2.0 * double(Jcd[k * ND + l]));
+            for (int l = 0; l < ND; ++l) atomicAdd(v.X + at(c0 + k, d0 + l), widen(Real(2) * Jcd[k * ND + l]));
     }
 }
 

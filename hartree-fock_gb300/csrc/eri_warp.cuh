@@ -324,13 +324,13 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
             if (o < NAB)
             {
                 for (int kl = 0; kl < NCD; ++kl) s += Es[o * NCD + kl] * ldD<Real>(v.Dt, at(c0 + kl / ND, d0 + kl % ND));
-                atomicAdd(v.X + at(a0 + o / NB, b0 + o % NB), 2.0 * double(s));
+                atomicAdd(v.X + at(a0 + o / NB, b0 + o % NB), widen(Real(2) * s));
             }
             else
             {
                 const int kl = o - NAB;
                 for (int ij = 0; ij < NAB; ++ij) s += Es[ij * NCD + kl] * ldD<Real>(v.Dt, at(a0 + ij / NB, b0 + ij % NB));
-                atomicAdd(v.X + at(c0 + kl / ND, d0 + kl % ND), 2.0 * double(s));
+                atomicAdd(v.X + at(c0 + kl / ND, d0 + kl % ND), widen(Real(2) * s));
             }
         }
         // K blocks: ac, ad, bc, bd.
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
                     for (int j = 0; j < NB; ++j)
                         for (int l = 0; l < ND; ++l)
                             s += Es[(i * NB + j) * NCD + k * ND + l] * ldD<Real>(Ds, at(b0 + j, d0 + l));
-                    atomicAdd(Yo + at(a0 + i, c0 + k), double(s));
+                    atomicAdd(Yo + at(a0 + i, c0 + k), widen(s));
                 }
                 else if (o < NA * NC + NA * ND)
                 {
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
                     for (int j = 0; j < NB; ++j)
                         for (int k = 0; k < NC; ++k)
                             s += Es[(i * NB + j) * NCD + k * ND + l] * ldD<Real>(Ds, at(b0 + j, c0 + k));
-                    atomicAdd(Yo + at(a0 + i, d0 + l), double(s));
+                    atomicAdd(Yo + at(a0 + i, d0 + l), widen(s));
                 }
                 else if (o < NA * NC + NA * ND + NB * NC)
                 {
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
                     for (int i = 0; i < NA; ++i)
                         for (int l = 0; l < ND; ++l)
                             s += Es[(i * NB + j) * NCD + k * ND + l] * ldD<Real>(Ds, at(a0 + i, d0 + l));
-                    atomicAdd(Yo + at(b0 + j, c0 + k), double(s));
+                    atomicAdd(Yo + at(b0 + j, c0 + k), widen(s));
                 }
                 else
                 {
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(32 * kWarpKernelWarps)
                     for (int i = 0; i < NA; ++i)
                         for (int k = 0; k < NC; ++k)
                             s += Es[(i * NB + j) * NCD + k * ND + l] * ldD<Real>(Ds, at(a0 + i, c0 + k));
-                    atomicAdd(Yo + at(b0 + j, d0 + l), double(s));
+                    atomicAdd(Yo + at(b0 + j, d0 + l), widen(s));
                 }
             }
         }
