@@ -138,7 +138,8 @@ cudaError_t HFG_CAT(launch_grad_, HFG_QCLASS)(const GradLaunch& c)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kGradWarps, smem);
     if (e != cudaSuccess)
         return e;
-    const unsigned long long need = (c.count + kGradWarps - 1) / kGradWarps;
+    constexpr unsigned long long per_block = kGradWarps * (32 / W::kGroup); // quartets in flight per block
+    const unsigned long long need = (c.count + per_block - 1) / per_block;
     const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
     kern<<<static_cast<unsigned>(need < cap ? need : cap), 32 * kGradWarps, smem, c.stream>>>(
         c.list, c.count, c.view, c.boys_slice, c.tables);

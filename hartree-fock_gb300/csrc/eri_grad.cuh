@@ -15,7 +15,8 @@
 //   X[ij][tuv'] = sum_{tuv} E^{ij}_{tuv} R_{t+tau,..}   (tau+nu+phi <= l_cd + 1)
 //   h[kl][tuv'] = sum_ij Gamma_ijkl X[ij][tuv']         -> g_C += (-1)^{..} DC . h
 // and g_D = -(g_A + g_B + g_C) (translational invariance).  E/R tables are recomputed here, nothing from
-// the forward build is stored.  One warp per quartet; FP64.
+// the forward build is stored.  One group of lanes per quartet (GradLayout::kGroup: 4 to 32 lanes by
+// class size; the groups of a warp work independently, synchronised by group masks); FP64.
 #pragma once
 
 #include "eri_warp.cuh"
@@ -52,7 +53,12 @@ template <int LA, int LB, int LC, int LD> struct GradLayout
     static constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD + 1;
     static constexpr int HAB1 = nherm(LAB + 1), HCD1 = nherm(LCD + 1), HL = nherm(L);
     static constexpr int kR = 2 * HL, kG = HAB1 * NCD, kX = NAB * HCD1, kGam = NAB * NCD;
-    static constexpr int kPerWarp = ((kR + kG + kX + kGam + 1) / 2) * 2;
+    // Lanes per quartet: a power of two from 4 to 32, about a quarter of the larger per-quartet work array,
+    // so that the small classes do not leave most of a warp idle; a warp holds 32 / kGroup quartets.
+    static constexpr int kWork  = kG > kX ? kG : kX;
+    static constexpr int kGroup = kWork <= 16 ? 4 : kWork <= 32 ? 8 : kWork <= 64 ? 16 : 32;
+    static constexpr int kPerGroup = ((kR + kG + kX + kGam + 1) / 2) * 2;
+    static constexpr int kPerWarp  = kPerGroup * (32 / kGroup);
 };
 
 constexpr int kGradWarps = 2;
@@ -77,21 +83,24 @@ __global__ void __launch_bounds__(32 * kGradWarps)
     constexpr int S = L + 1;
     constexpr int G1B = g1d_size(LA, LB), G1K = g1d_size(LC, LD);
 
+    constexpr int GS = W::kGroup, NG = 32 / GS; // lanes per quartet, quartets per warp
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* slice = reinterpret_cast<double*>(smem_raw);
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    if (static_cast<unsigned long long>(blockIdx.x) * kGradWarps >= n)
+    const int wl = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int lane = wl % GS, grp = wl / GS; // lane within the quartet's group, group within the warp
+    const unsigned gmask = (GS == 32) ? 0xffffffffu : (((1u << GS) - 1u) << (grp * GS));
+    if (static_cast<unsigned long long>(blockIdx.x) * kGradWarps * NG >= n)
         return;
     stage_boys<double>(boys_slice, slice);
-    double* wbase = slice + BoysGrid<double>::kPoints * BoysGrid<double>::kRow + wib * W::kPerWarp;
+    double* wbase = slice + BoysGrid<double>::kPoints * BoysGrid<double>::kRow + wib * W::kPerWarp + grp * W::kPerGroup;
     double* Rbuf0 = wbase;
     double* Rbuf1 = wbase + HL;
     double* Gs    = wbase + 2 * HL;
     double* Xs    = Gs + W::kG;
     double* Gam   = Xs + W::kX;
 
-    for (unsigned long long q = static_cast<unsigned long long>(blockIdx.x) * kGradWarps + wib; q < n;
-         q += static_cast<unsigned long long>(gridDim.x) * kGradWarps)
+    for (unsigned long long q = (static_cast<unsigned long long>(blockIdx.x) * kGradWarps + wib) * NG + grp; q < n;
+         q += static_cast<unsigned long long>(gridDim.x) * kGradWarps * NG)
     {
         const Quartet qt  = list[q];
         const PairRec bra = v.pairs[qt.bra];
@@ -100,7 +109,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
         const int n = v.n;
         const double sdeg = 4.0 * (bra.same ? 0.5 : 1.0) * (ket.same ? 0.5 : 1.0) * (qt.bra == qt.ket ? 0.5 : 1.0);
         // Gamma (with the angular normalisation of the four components and the degeneracy factor).
-        for (int e = lane; e < NAB * NCD; e += 32)
+        for (int e = lane; e < NAB * NCD; e += GS)
         {
             const int ij = e / NCD, kl = e % NCD;
             const int i = ij / NB, j = ij % NB, k = kl / ND, l = kl % ND;
@@ -111,7 +120,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                                     D(v.Db, I, K) * D(v.Db, J, Lx) + D(v.Db, I, Lx) * D(v.Db, J, K));
             Gam[e] = sdeg * ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k) * ang_norm(LD, l) * g;
         }
-        __syncwarp();
+        __syncwarp(gmask);
         double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
 
         for (int ib = 0; ib < bra.npp; ++ib)
@@ -148,12 +157,12 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                 double* dst = Rbuf1;
                 if (lane == 0)
                     src[0] = Fs[L];
-                __syncwarp();
+                __syncwarp(gmask);
 #pragma unroll
                 for (int lev = L - 1; lev >= 0; --lev)
                 {
                     const int cnt = nherm(L - lev);
-                    for (int k = 1 + lane; k < cnt; k += 32)
+                    for (int k = 1 + lane; k < cnt; k += GS)
                     {
                         const int4 r  = tabs->rtab[L][k];
                         const int ax  = r.w & 3, c = r.w >> 2;
@@ -165,7 +174,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     }
                     if (lane == 0)
                         dst[0] = Fs[lev];
-                    __syncwarp();
+                    __syncwarp(gmask);
                     double* t = src;
                     src       = dst;
                     dst       = t;
@@ -174,7 +183,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                 auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
 
                 // G[tuv][kl] over t+u+v <= LAB+1, and X[ij][tuv'] over t+u+v <= LCD+1.
-                for (int e = lane; e < HAB1 * NCD; e += 32)
+                for (int e = lane; e < HAB1 * NCD; e += GS)
                 {
                     const int h = e / NCD, kl = e % NCD;
                     const int tuv = tabs->htuv[LAB + 1][h];
@@ -198,7 +207,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                         }
                     Gs[e] = s;
                 }
-                for (int e = lane; e < NAB * HCD1; e += 32)
+                for (int e = lane; e < NAB * HCD1; e += GS)
                 {
                     const int ij = e / HCD1, h = e % HCD1;
                     const int tuv = tabs->htuv[LCD + 1][h];
@@ -219,9 +228,9 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                         }
                     Xs[e] = s;
                 }
-                __syncwarp();
+                __syncwarp(gmask);
                 // Bra centres A, B.
-                for (int e = lane; e < NAB * HAB1; e += 32)
+                for (int e = lane; e < NAB * HAB1; e += GS)
                 {
                     const int ij = e / HAB1, h = e % HAB1;
                     double y = 0.0;
@@ -252,7 +261,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     gB[2] += y * f[0] * f[1] * dB[2];
                 }
                 // Ket centre C.
-                for (int e = lane; e < NCD * HCD1; e += 32)
+                for (int e = lane; e < NCD * HCD1; e += GS)
                 {
                     const int kl = e / HCD1, h = e % HCD1;
                     double hv = 0.0;
@@ -279,15 +288,15 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     gC[1] += hv * f[0] * dC[1] * f[2];
                     gC[2] += hv * f[0] * f[1] * dC[2];
                 }
-                __syncwarp();
+                __syncwarp(gmask);
             }
         }
         for (int x = 0; x < 3; ++x)
-            for (int o = 16; o > 0; o >>= 1)
+            for (int o = GS / 2; o > 0; o >>= 1)
             {
-                gA[x] += __shfl_down_sync(0xffffffffu, gA[x], o);
-                gB[x] += __shfl_down_sync(0xffffffffu, gB[x], o);
-                gC[x] += __shfl_down_sync(0xffffffffu, gC[x], o);
+                gA[x] += __shfl_down_sync(gmask, gA[x], o, GS);
+                gB[x] += __shfl_down_sync(gmask, gB[x], o, GS);
+                gC[x] += __shfl_down_sync(gmask, gC[x], o, GS);
             }
         if (lane == 0)
         {
@@ -301,7 +310,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                 atomicAdd(v.grad + 3 * td + x, -(gA[x] + gB[x] + gC[x]));
             }
         }
-        __syncwarp();
+        __syncwarp(gmask);
     }
 }
 #endif
