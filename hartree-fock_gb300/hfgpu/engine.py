@@ -199,13 +199,20 @@ class Engine:
         Q = np.asfortranarray(Q, dtype=np.float64).ravel(order="F")
         self._check(lib().hfg_set_schwartz(self.h, _dp(Q)))
 
-    def fock(self, dD_tot, dD_alpha, dD_beta=None, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-4):
-        """(J, Ka, Kb or None, stats dict) for host numpy matrices (single molecule: n x n)."""
+    def fock(self, dD_tot, dD_alpha, dD_beta=None, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-4,
+             out=None):
+        """(J, Ka, Kb or None, stats dict) for host numpy matrices (single molecule: n x n).  `out`: optional
+        caller-owned flat float64 host buffers [J, Ka(, Kb)] (e.g. pinned memory) that receive the result."""
         uhf = dD_beta is not None
         flat = lambda x: np.asfortranarray(x, dtype=np.float64).ravel(order="F")
         ins = [flat(dD_tot), flat(dD_alpha), flat(dD_beta) if uhf else None]
         size = ins[0].size
-        outs = [np.zeros(size) for _ in range(3 if uhf else 2)] + ([] if uhf else [None])
+        if out is not None:
+            outs = list(out) + ([] if uhf else [None])
+            if any(o.dtype != np.float64 or o.size != size or not o.flags.c_contiguous for o in outs if o is not None):
+                raise ValueError("fock: out buffers must be contiguous float64 arrays of the matrix size")
+        else:
+            outs = [np.zeros(size) for _ in range(3 if uhf else 2)] + ([] if uhf else [None])
         req = _Request(1 if uhf else 0, precision, 0, sthr, dthr, fp32_cutoff,
                        *[x.ctypes.data if x is not None else None for x in ins],
                        *[x.ctypes.data if x is not None else None for x in outs])

@@ -114,3 +114,18 @@ def test_gpu_batch_equals_single_molecules():
         Kb = K[off:off + n * n].reshape(n, n, order="F")
         assert np.max(np.abs(Jb - J1)) <= 1e-12 and np.max(np.abs(Kb - K1)) <= 1e-12
         off += n * n
+
+
+def test_gpu_fock_into_caller_buffers():
+    from hfgpu.engine import Engine
+
+    g = load_golden("w2_631gss")
+    e = Engine(g["soa"])
+    Da = g["Da"]
+    J, K, _, _ = e.fock(2 * Da, Da)
+    out = [np.full(Da.size, np.nan), np.full(Da.size, np.nan)]
+    J2, K2, _, _ = e.fock(2 * Da, Da, out=out)
+    assert np.shares_memory(J2, out[0]) and np.shares_memory(K2, out[1])
+    assert np.max(np.abs(J2 - J)) <= 1e-12 and np.max(np.abs(K2 - K)) <= 1e-12
+    with pytest.raises(ValueError):
+        e.fock(2 * Da, Da, out=[np.zeros(3), np.zeros(3)])
