@@ -385,8 +385,9 @@ def gpu_arm(args, dist):
 
 
 def scf_timings(soa, Z, xyz, dev, cutoff):
-    """Full SCFs of the workload: RHF in FP64 and mixed precision (the headline speed-up), the nuclear
-    gradient after the mixed RHF SCF, and the +1 doublet UHF (GUESS_MIX 2) in FP64 and mixed precision."""
+    """Full SCFs of the workload: RHF in FP64 and mixed precision (the headline speed-up), the mixed-precision
+    nuclear gradient after the mixed SCFs (for RHF also the FP64 gradient on the same densities), and the
+    +1 doublet UHF (GUESS_MIX 2) in FP64 and mixed precision."""
     import numpy as np
 
     from hfgpu.engine import FP64, MIXED, Engine
@@ -401,14 +402,21 @@ def scf_timings(soa, Z, xyz, dev, cutoff):
         if mult != 1:
             out["s_squared"] = r["s_squared"]
         if grad:
+            # The mixed SCF's gradient: small-bound quartets' derivative integrals in FP32; against the FP64
+            # gradient on the same densities when grad == "both".
             t0 = time.perf_counter()
-            g, ms2 = eng.gradient(Z, xyz, unrestricted=mult != 1)
-            out["gradient"] = {"seconds": time.perf_counter() - t0, "two_electron_ms": ms2,
+            g, ms2 = eng.gradient(Z, xyz, unrestricted=mult != 1, precision=MIXED, fp32_cutoff=cutoff)
+            out["gradient"] = {"precision": "mixed", "seconds": time.perf_counter() - t0, "two_electron_ms": ms2,
                                "max_abs": float(np.abs(g).max()), "sum_abs_translation": float(np.abs(g.sum(0)).max())}
+            if grad == "both":
+                t0 = time.perf_counter()
+                g64, ms64 = eng.gradient(Z, xyz, unrestricted=mult != 1)
+                out["gradient"]["fp64_seconds"] = time.perf_counter() - t0
+                out["gradient"]["max_abs_vs_fp64_gradient"] = float(np.abs(g - g64).max())
         eng.close()
         return out
 
-    res = {"rhf": {"fp64": one(FP64, 0, 1, False), "mixed": one(MIXED, 0, 1, True)},
+    res = {"rhf": {"fp64": one(FP64, 0, 1, False), "mixed": one(MIXED, 0, 1, "both")},
            "uhf_cation_doublet": {"fp64": one(FP64, 1, 2, False), "mixed": one(MIXED, 1, 2, True)}}
     for k in res:
         res[k]["delta_e"] = abs(res[k]["mixed"]["e_total"] - res[k]["fp64"]["e_total"])

@@ -124,13 +124,13 @@ unsigned HFG_CAT(class_form_mask_, HFG_QCLASS)(bool fp32)
     return form_mask(fp32) | (static_cast<unsigned>(warp_form(fp32) ? kFormWarp : kFormThread) << 16);
 }
 
-cudaError_t HFG_CAT(launch_grad_, HFG_QCLASS)(const GradLaunch& c)
+namespace
 {
-    if (c.count == 0)
-        return cudaSuccess;
+template <typename Real> cudaError_t launch_grad_t(const GradLaunch& c)
+{
     using W           = GradLayout<LA, LB, LC, LD>;
-    const size_t smem = sizeof(double) * (BoysGrid<double>::kPoints * BoysGrid<double>::kRow + W::kPerWarp * kGradWarps);
-    auto kern         = grad_class_kernel<LA, LB, LC, LD>;
+    const size_t smem = sizeof(Real) * (BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow + W::kPerWarp * kGradWarps);
+    auto kern         = grad_class_kernel<LA, LB, LC, LD, Real>;
     cudaError_t e     = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess)
         return e;
@@ -142,7 +142,15 @@ cudaError_t HFG_CAT(launch_grad_, HFG_QCLASS)(const GradLaunch& c)
     const unsigned long long need = (c.count + per_block - 1) / per_block;
     const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
     kern<<<static_cast<unsigned>(need < cap ? need : cap), 32 * kGradWarps, smem, c.stream>>>(
-        c.list, c.count, c.view, c.boys_slice, c.tables);
+        c.list, c.count, c.view, static_cast<const Real*>(c.boys_slice), c.tables);
     return cudaGetLastError();
+}
+} // namespace
+
+cudaError_t HFG_CAT(launch_grad_, HFG_QCLASS)(const GradLaunch& c)
+{
+    if (c.count == 0)
+        return cudaSuccess;
+    return c.fp32 ? launch_grad_t<float>(c) : launch_grad_t<double>(c);
 }
 } // namespace hfg

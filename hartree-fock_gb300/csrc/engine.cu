@@ -140,6 +140,7 @@ struct hfg_engine
     std::vector<int> npp_full, keep_off, keep_idx;
     // Unscreened records in pack order (the nuclear gradient's derivative integrals use every primitive).
     hfg::DevBuf<double> d_pptab64_full[hfg::kNumPairClasses];
+    hfg::DevBuf<float> d_pptab32_full[hfg::kNumPairClasses];
     hfg::DevBuf<hfg::PairRec> d_gspairs; // sorted order, npp_full, pp_off = orig_off
     hfg::DevBuf<long long> d_mat_off;
     hfg::DevBuf<int> d_mat_ld;
@@ -150,6 +151,7 @@ struct hfg_engine
     hfg::DevBuf<double> d_boys64[hfg::kMaxLt + 2];
     hfg::DevBuf<float> d_boys32[hfg::kMaxLt + 2];
     hfg::DevBuf<double> d_gtab[hfg::kNumPairClasses]; // gradient records (built on first use)
+    hfg::DevBuf<float> d_gtab32[hfg::kNumPairClasses]; // their FP32 copies (mixed-precision gradient)
     bool have_gtab = false;
     hfg::DevBuf<int> d_shell_atom;
     hfg::DevBuf<double> d_grad;
@@ -852,6 +854,7 @@ static void pack_molecules(hfg_engine* e)
     {
         e->h_tab[pc] = std::move(tab[pc]);
         e->d_pptab64_full[pc].upload(e->h_tab[pc], e->stream);
+        e->d_pptab32_full[pc].upload(std::vector<float>(e->h_tab[pc].begin(), e->h_tab[pc].end()), e->stream);
     }
     e->keep_off.assign(e->pairs.size() + 1, 0);
     e->keep_idx.clear();
@@ -1582,48 +1585,72 @@ static void build_grad_tables(hfg_engine* e)
                 }
             }
     }
-    for (int pc = 0; pc < kNumPairClasses; ++pc) e->d_gtab[pc].upload(tab[pc], e->stream);
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        e->d_gtab[pc].upload(tab[pc], e->stream);
+        e->d_gtab32[pc].upload(std::vector<float>(tab[pc].begin(), tab[pc].end()), e->stream);
+    }
     HFG_CUDA(cudaStreamSynchronize(e->stream));
     e->have_gtab = true;
 }
 
 // Two-electron part of the nuclear gradient on the device (eri_grad.cuh) for the densities in
-// d_dD[0..2] (total, alpha, beta); adds into grad[3*natom] (host).  Returns the device milliseconds.
+// d_dD[0..2] (total, alpha, beta); adds into grad[3*natom] (host).  mixed: quartets whose bound
+// Q_ab Q_cd max|D| is below `cutoff` run in the FP32 kernels (the Fock build's split), the rest in FP64;
+// every contribution accumulates in FP64.  Returns the device milliseconds.
 static double gradient_two_electron(hfg_engine* e, const std::vector<int>& shell_atom, int natom, bool uhf,
-                                    double sthr, double dthr, double* grad)
+                                    double sthr, double dthr, bool mixed, double cutoff, double* grad)
 {
     cudaStream_t s = e->stream;
     build_grad_tables(e);
     e->d_shell_atom.upload(shell_atom, s);
     e->d_grad.alloc(static_cast<size_t>(3) * natom);
     HFG_CUDA(cudaMemsetAsync(e->d_grad.p, 0, sizeof(double) * 3 * natom, s));
-    size_lists(e, sthr, false);
-    build_lists(e, uhf, false, sthr, dthr, 0.0);
-    GradView v {};
-    v.pairs = e->d_gspairs.p;
-    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    const long long N2 = e->mat_total;
+    if (mixed)
+        for (int k = 0; k < 3; ++k)
+        {
+            if (!e->d_dDf[k].p)
+            {
+                invalidate_graph(e);
+                e->d_dDf[k].alloc(N2);
+            }
+            to_float_kernel<<<grid_for(N2, 256, e->num_sms), 256, 0, s>>>(e->d_dD[k].p, e->d_dDf[k].p, N2);
+            HFG_CUDA(cudaGetLastError());
+        }
+    size_lists(e, sthr, mixed);
+    build_lists(e, uhf, mixed, sthr, dthr, cutoff);
+    GradView v[2] {};
+    for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
     {
-        v.pptab[pc] = e->d_pptab64_full[pc].p;
-        v.gtab[pc]  = e->d_gtab[pc].p;
+        GradView& g = v[prec];
+        g.pairs     = e->d_gspairs.p;
+        for (int pc = 0; pc < kNumPairClasses; ++pc)
+        {
+            g.pptab[pc] = prec ? static_cast<const void*>(e->d_pptab32_full[pc].p) : e->d_pptab64_full[pc].p;
+            g.gtab[pc]  = prec ? static_cast<const void*>(e->d_gtab32[pc].p) : e->d_gtab[pc].p;
+        }
+        g.Dt = prec ? static_cast<const void*>(e->d_dDf[0].p) : e->d_dD[0].p;
+        g.Da = prec ? static_cast<const void*>(e->d_dDf[1].p) : e->d_dD[1].p;
+        g.Db = uhf ? (prec ? static_cast<const void*>(e->d_dDf[2].p) : e->d_dD[2].p) : g.Da;
+        g.n          = e->mols[0].nao;
+        g.shell_atom = e->d_shell_atom.p;
+        g.grad       = e->d_grad.p;
     }
-    v.Dt = e->d_dD[0].p;
-    v.Da = e->d_dD[1].p;
-    v.Db = uhf ? e->d_dD[2].p : e->d_dD[1].p;
-    v.n = e->mols[0].nao;
-    v.shell_atom = e->d_shell_atom.p;
-    v.grad = e->d_grad.p;
     HFG_CUDA(cudaEventRecord(e->ev[6], s));
-    for (int qc = kNumQuartetClasses - 1; qc >= 0; --qc)
-    {
-        const unsigned long long n = e->h_counts[2 * qc];
-        if (n == 0)
-            continue;
-        const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
-        const int P2 = qc - P1 * (P1 + 1) / 2;
-        const int L  = pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2);
-        GradLaunch g {e->d_list[qc][0].p, n, v, e->d_boys64[L + 1].p, e->d_tables.p, s, e->num_sms};
-        HFG_CUDA(launch_grad(qc, g));
-    }
+    for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
+        for (int qc = kNumQuartetClasses - 1; qc >= 0; --qc)
+        {
+            const unsigned long long n = e->h_counts[2 * qc + prec];
+            if (n == 0)
+                continue;
+            const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+            const int P2 = qc - P1 * (P1 + 1) / 2;
+            const int L  = pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2);
+            const void* slice = prec ? static_cast<const void*>(e->d_boys32[L + 1].p) : e->d_boys64[L + 1].p;
+            GradLaunch g {e->d_list[qc][prec].p, n, v[prec], slice, e->d_tables.p, s, e->num_sms, prec == 1};
+            HFG_CUDA(launch_grad(qc, g));
+        }
     HFG_CUDA(cudaEventRecord(e->ev[7], s));
     std::vector<double> g(static_cast<size_t>(3) * natom);
     HFG_CUDA(cudaMemcpyAsync(g.data(), e->d_grad.p, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s));
@@ -2024,6 +2051,10 @@ int hfg_gradient(hfg_engine* e, const hfg_gradient_request* r, double* grad, dou
     return guarded(e, [&] {
         if (e->nmol != 1)
             throw HfgError(HFG_ERR_INVALID, "hfg_gradient: the engine must hold exactly one molecule");
+        if (r->precision != HFG_PRECISION_FP64 && r->precision != HFG_PRECISION_MIXED)
+            throw HfgError(HFG_ERR_INVALID, "hfg_gradient: unknown precision mode");
+        if (r->precision == HFG_PRECISION_MIXED && !(r->fp32_cutoff >= 0.0 && std::isfinite(r->fp32_cutoff)))
+            throw HfgError(HFG_ERR_INVALID, "hfg_gradient: fp32_cutoff must be finite and >= 0");
         HFG_CUDA(cudaSetDevice(e->device));
         const int n = e->mols[0].nao;
         const size_t N2 = static_cast<size_t>(n) * n;
@@ -2068,7 +2099,8 @@ int hfg_gradient(hfg_engine* e, const hfg_gradient_request* r, double* grad, dou
         HFG_CUDA(cudaMemcpyAsync(e->d_dD[2].p, Db, sizeof(double) * N2, cudaMemcpyHostToDevice, e->stream));
         std::fill(grad, grad + 3 * r->natom, 0.0);
         const double ms = hfg::gradient_two_electron(e, shell_atom, r->natom, true, r->schwartz_threshold,
-                                                     r->density_threshold, grad);
+                                                     r->density_threshold, r->precision == HFG_PRECISION_MIXED,
+                                                     r->fp32_cutoff, grad);
         if (ms_two_electron)
             *ms_two_electron = ms;
         e->last_valid = false; // the lists now hold the gradient's quartets

@@ -43,10 +43,11 @@ struct GradLaunch
     const Quartet* list;
     unsigned long long count;
     const GradView& view;
-    const double* boys_slice; // slice for total L + 1
+    const void* boys_slice; // slice for total L + 1, Real of the kernel
     const WarpTables* tables;
     cudaStream_t stream;
     int num_sms;
+    bool fp32;
 };
 cudaError_t launch_grad(int qclass, const GradLaunch& L);
 

@@ -15,8 +15,9 @@
 //   X[ij][tuv'] = sum_{tuv} E^{ij}_{tuv} R_{t+tau,..}   (tau+nu+phi <= l_cd + 1)
 //   h[kl][tuv'] = sum_ij Gamma_ijkl X[ij][tuv']         -> g_C += (-1)^{..} DC . h
 // and g_D = -(g_A + g_B + g_C) (translational invariance).  E/R tables are recomputed here, nothing from
-// the forward build is stored.  One group of lanes per quartet (GradLayout::kGroup: 4 to 32 lanes by
-// class size; the groups of a warp work independently, synchronised by group masks); FP64.
+// the forward build is stored.  FP64, or FP32 for the small-bound quartets of a mixed-precision gradient
+// (FP64 accumulation).  One group of lanes per quartet (GradLayout::kGroup: 4 to 32 lanes by
+// class size; the groups of a warp work independently, synchronised by group masks).
 #pragma once
 
 #include "eri_warp.cuh"
@@ -35,11 +36,11 @@ __host__ __device__ constexpr int g_stride(int l1, int l2)
 struct GradView
 {
     const PairRec* pairs;
-    const double* pptab[kNumPairClasses]; // forward records (p, P, W, ...)
-    const double* gtab[kNumPairClasses];  // gradient records
-    const double* Dt;
-    const double* Da;
-    const double* Db;
+    const void* pptab[kNumPairClasses]; // forward records (p, P, W, ...), Real of the kernel
+    const void* gtab[kNumPairClasses];  // gradient records, Real of the kernel
+    const void* Dt;                     // densities, Real of the kernel
+    const void* Da;
+    const void* Db;
     int n;                  // nao
     const int* shell_atom;  // per shell
     double* grad;           // [natom][3]
@@ -63,16 +64,25 @@ template <int LA, int LB, int LC, int LD> struct GradLayout
 
 constexpr int kGradWarps = 2;
 
-__device__ __forceinline__ double e1(const double* T, int l2, int l12, int i, int j, int t)
+// Angular normalisation factor of component c of l in the kernel's precision (integer tests and selects
+// only: no double arithmetic in the FP32 kernels).
+template <typename Real> __device__ __forceinline__ Real ang_norm_r(int l, int c)
+{
+    const int i = cart_exp(l, c, 0), j = cart_exp(l, c, 1), k = cart_exp(l, c, 2);
+    const int d = dfact_odd(2 * i - 1) * dfact_odd(2 * j - 1) * dfact_odd(2 * k - 1);
+    return d == 1 ? Real(1) : (d == 3 ? Real(0.57735026918962576451) : (d == 9 ? Real(1.0 / 3.0) : (d == 15 ? Real(0.25819888974716112568) : Real(1))));
+}
+
+template <typename Real> __device__ __forceinline__ Real e1(const Real* T, int l2, int l12, int i, int j, int t)
 {
     // T: one axis of a gradient record, dense [i][j][t] with extents (l1+2, l2+2, l12+3)
     return T[(i * (l2 + 2) + j) * (l12 + 3) + t];
 }
 
-template <int LA, int LB, int LC, int LD>
+template <int LA, int LB, int LC, int LD, typename Real>
 __global__ void __launch_bounds__(32 * kGradWarps)
     grad_class_kernel(const Quartet* __restrict__ list, unsigned long long n, GradView v,
-                      const double* __restrict__ boys_slice, const WarpTables* __restrict__ tabs)
+                      const Real* __restrict__ boys_slice, const WarpTables* __restrict__ tabs)
 {
     using W = GradLayout<LA, LB, LC, LD>;
     constexpr int NA = W::NA, NB = W::NB, NC = W::NC, ND = W::ND, NAB = W::NAB, NCD = W::NCD;
@@ -85,19 +95,22 @@ __global__ void __launch_bounds__(32 * kGradWarps)
 
     constexpr int GS = W::kGroup, NG = 32 / GS; // lanes per quartet, quartets per warp
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double* slice = reinterpret_cast<double*>(smem_raw);
+    Real* slice = reinterpret_cast<Real*>(smem_raw);
     const int wl = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int lane = wl % GS, grp = wl / GS; // lane within the quartet's group, group within the warp
     const unsigned gmask = (GS == 32) ? 0xffffffffu : (((1u << GS) - 1u) << (grp * GS));
     if (static_cast<unsigned long long>(blockIdx.x) * kGradWarps * NG >= n)
         return;
-    stage_boys<double>(boys_slice, slice);
-    double* wbase = slice + BoysGrid<double>::kPoints * BoysGrid<double>::kRow + wib * W::kPerWarp + grp * W::kPerGroup;
-    double* Rbuf0 = wbase;
-    double* Rbuf1 = wbase + HL;
-    double* Gs    = wbase + 2 * HL;
-    double* Xs    = Gs + W::kG;
-    double* Gam   = Xs + W::kX;
+    stage_boys<Real>(boys_slice, slice);
+    Real* wbase = slice + BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow + wib * W::kPerWarp + grp * W::kPerGroup;
+    Real* Rbuf0 = wbase;
+    Real* Rbuf1 = wbase + HL;
+    Real* Gs    = wbase + 2 * HL;
+    Real* Xs    = Gs + W::kG;
+    Real* Gam   = Xs + W::kX;
+    const Real* Dt = static_cast<const Real*>(v.Dt);
+    const Real* Da = static_cast<const Real*>(v.Da);
+    const Real* Db = static_cast<const Real*>(v.Db);
 
     for (unsigned long long q = (static_cast<unsigned long long>(blockIdx.x) * kGradWarps + wib) * NG + grp; q < n;
          q += static_cast<unsigned long long>(gridDim.x) * kGradWarps * NG)
@@ -107,45 +120,45 @@ __global__ void __launch_bounds__(32 * kGradWarps)
         const PairRec ket = v.pairs[qt.ket];
         const int a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
         const int n = v.n;
-        const double sdeg = 4.0 * (bra.same ? 0.5 : 1.0) * (ket.same ? 0.5 : 1.0) * (qt.bra == qt.ket ? 0.5 : 1.0);
+        const Real sdeg = Real(4) * (bra.same ? Real(0.5) : Real(1)) * (ket.same ? Real(0.5) : Real(1)) * (qt.bra == qt.ket ? Real(0.5) : Real(1));
         // Gamma (with the angular normalisation of the four components and the degeneracy factor).
         for (int e = lane; e < NAB * NCD; e += GS)
         {
             const int ij = e / NCD, kl = e % NCD;
             const int i = ij / NB, j = ij % NB, k = kl / ND, l = kl % ND;
             const long long I = a0 + i, J = b0 + j, K = c0 + k, Lx = d0 + l;
-            auto D = [&](const double* M, long long r, long long c) { return M[r + c * n]; };
-            const double g = D(v.Dt, I, J) * D(v.Dt, K, Lx) -
-                             0.5 * (D(v.Da, I, K) * D(v.Da, J, Lx) + D(v.Da, I, Lx) * D(v.Da, J, K) +
-                                    D(v.Db, I, K) * D(v.Db, J, Lx) + D(v.Db, I, Lx) * D(v.Db, J, K));
-            Gam[e] = sdeg * ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k) * ang_norm(LD, l) * g;
+            auto D = [&](const Real* M, long long r, long long c) { return M[r + c * n]; };
+            const Real g = D(Dt, I, J) * D(Dt, K, Lx) -
+                             Real(0.5) * (D(Da, I, K) * D(Da, J, Lx) + D(Da, I, Lx) * D(Da, J, K) +
+                                    D(Db, I, K) * D(Db, J, Lx) + D(Db, I, Lx) * D(Db, J, K));
+            Gam[e] = sdeg * ang_norm_r<Real>(LA, i) * ang_norm_r<Real>(LB, j) * ang_norm_r<Real>(LC, k) * ang_norm_r<Real>(LD, l) * g;
         }
         __syncwarp(gmask);
-        double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+        Real gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
 
         for (int ib = 0; ib < bra.npp; ++ib)
         {
-            const double* __restrict__ rb = v.pptab[PCB] + static_cast<size_t>(bra.pp_off + ib) * SB;
-            const double* __restrict__ gb = v.gtab[PCB] + static_cast<size_t>(bra.pp_off + ib) * GB;
-            const double p = rb[0], Px = rb[1], Py = rb[2], Pz = rb[3], Wab = rb[4];
-            const double aexp = gb[0], bexp = gb[1];
+            const Real* __restrict__ rb = static_cast<const Real*>(v.pptab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * SB;
+            const Real* __restrict__ gb = static_cast<const Real*>(v.gtab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * GB;
+            const Real p = rb[0], Px = rb[1], Py = rb[2], Pz = rb[3], Wab = rb[4];
+            const Real aexp = gb[0], bexp = gb[1];
             for (int ik = 0; ik < ket.npp; ++ik)
             {
-                const double* __restrict__ rk = v.pptab[PCK] + static_cast<size_t>(ket.pp_off + ik) * SK;
-                const double* __restrict__ gk = v.gtab[PCK] + static_cast<size_t>(ket.pp_off + ik) * GK;
-                const double qq = rk[0];
-                const double X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
-                const double rs   = hfg_rsqrt(p + qq);
-                const double rho  = (p * qq) * (rs * rs);
-                const double pref = (Wab * rk[4]) * rs;
-                const double T    = rho * (X * X + Y * Y + Z * Z);
-                const double cexp = gk[0];
-                double F[L + 1];
-                boys_eval<L, double>(T, slice, F);
-                double Fs[L + 1];
+                const Real* __restrict__ rk = static_cast<const Real*>(v.pptab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * SK;
+                const Real* __restrict__ gk = static_cast<const Real*>(v.gtab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * GK;
+                const Real qq = rk[0];
+                const Real X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
+                const Real rs   = hfg_rsqrt(p + qq);
+                const Real rho  = (p * qq) * (rs * rs);
+                const Real pref = (Wab * rk[4]) * rs;
+                const Real T    = rho * (X * X + Y * Y + Z * Z);
+                const Real cexp = gk[0];
+                Real F[L + 1];
+                boys_eval<L, Real>(T, slice, F);
+                Real Fs[L + 1];
                 {
-                    const double m2r = -2.0 * rho;
-                    double w         = pref;
+                    const Real m2r = Real(-2) * rho;
+                    Real w         = pref;
 #pragma unroll
                     for (int k = 0; k <= L; ++k)
                     {
@@ -153,8 +166,8 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                         w *= m2r;
                     }
                 }
-                double* src = Rbuf0;
-                double* dst = Rbuf1;
+                Real* src = Rbuf0;
+                Real* dst = Rbuf1;
                 if (lane == 0)
                     src[0] = Fs[L];
                 __syncwarp(gmask);
@@ -166,20 +179,25 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     {
                         const int4 r  = tabs->rtab[L][k];
                         const int ax  = r.w & 3, c = r.w >> 2;
-                        const double xa = ax == 0 ? X : (ax == 1 ? Y : Z);
-                        double val    = xa * src[r.y];
+                        const Real xa = ax == 0 ? X : (ax == 1 ? Y : Z);
+                        Real val    = xa * src[r.y];
                         if (c > 0)
-                            val = fma(tabs->rcoef[L][k], src[r.z], val);
+                        {
+                            if constexpr (sizeof(Real) == 8)
+                                val = fma(tabs->rcoef[L][k], src[r.z], val);
+                            else
+                                val = fmaf(Real(c), src[r.z], val);
+                        }
                         dst[r.x] = val;
                     }
                     if (lane == 0)
                         dst[0] = Fs[lev];
                     __syncwarp(gmask);
-                    double* t = src;
+                    Real* t = src;
                     src       = dst;
                     dst       = t;
                 }
-                const double* R = src;
+                const Real* R = src;
                 auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
 
                 // G[tuv][kl] over t+u+v <= LAB+1, and X[ij][tuv'] over t+u+v <= LCD+1.
@@ -191,17 +209,17 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     const int k = kl / ND, l = kl % ND;
                     const int kx = cart_exp(LC, k, 0), ky = cart_exp(LC, k, 1), kz = cart_exp(LC, k, 2);
                     const int lx = cart_exp(LD, l, 0), ly = cart_exp(LD, l, 1), lz = cart_exp(LD, l, 2);
-                    const double* Ex = gk + 2;
-                    const double* Ey = Ex + G1K;
-                    const double* Ez = Ey + G1K;
-                    double s = 0.0;
+                    const Real* Ex = gk + 2;
+                    const Real* Ey = Ex + G1K;
+                    const Real* Ez = Ey + G1K;
+                    Real s = Real(0);
                     for (int ph = 0; ph <= kz + lz; ++ph)
                         for (int nu = 0; nu <= ky + ly; ++nu)
                         {
-                            const double eyz = e1(Ey, LD, LCD, ky, ly, nu) * e1(Ez, LD, LCD, kz, lz, ph);
+                            const Real eyz = e1(Ey, LD, LCD, ky, ly, nu) * e1(Ez, LD, LCD, kz, lz, ph);
                             for (int ta = 0; ta <= kx + lx; ++ta)
                             {
-                                const double ek = eyz * e1(Ex, LD, LCD, kx, lx, ta);
+                                const Real ek = eyz * e1(Ex, LD, LCD, kx, lx, ta);
                                 s = fma(((ta + nu + ph) & 1) ? -ek : ek, Ridx(t + ta, u + nu, w_ + ph), s);
                             }
                         }
@@ -215,14 +233,14 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     const int i = ij / NB, j = ij % NB;
                     const int ix = cart_exp(LA, i, 0), iy = cart_exp(LA, i, 1), iz = cart_exp(LA, i, 2);
                     const int jx = cart_exp(LB, j, 0), jy = cart_exp(LB, j, 1), jz = cart_exp(LB, j, 2);
-                    const double* Ex = gb + 2;
-                    const double* Ey = Ex + G1B;
-                    const double* Ez = Ey + G1B;
-                    double s = 0.0;
+                    const Real* Ex = gb + 2;
+                    const Real* Ey = Ex + G1B;
+                    const Real* Ez = Ey + G1B;
+                    Real s = Real(0);
                     for (int w_ = 0; w_ <= iz + jz; ++w_)
                         for (int u = 0; u <= iy + jy; ++u)
                         {
-                            const double eyz = e1(Ey, LB, LAB, iy, jy, u) * e1(Ez, LB, LAB, iz, jz, w_);
+                            const Real eyz = e1(Ey, LB, LAB, iy, jy, u) * e1(Ez, LB, LAB, iz, jz, w_);
                             for (int t = 0; t <= ix + jx; ++t)
                                 s += eyz * e1(Ex, LB, LAB, ix, jx, t) * Ridx(t + ta, u + nu, w_ + ph);
                         }
@@ -233,25 +251,25 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                 for (int e = lane; e < NAB * HAB1; e += GS)
                 {
                     const int ij = e / HAB1, h = e % HAB1;
-                    double y = 0.0;
+                    Real y = Real(0);
                     for (int kl = 0; kl < NCD; ++kl) y += Gam[ij * NCD + kl] * Gs[h * NCD + kl];
-                    if (y == 0.0)
+                    if (y == Real(0))
                         continue;
                     const int tuv = tabs->htuv[LAB + 1][h];
                     const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
                     const int i = ij / NB, j = ij % NB;
                     const int ie[3] = {cart_exp(LA, i, 0), cart_exp(LA, i, 1), cart_exp(LA, i, 2)};
                     const int je[3] = {cart_exp(LB, j, 0), cart_exp(LB, j, 1), cart_exp(LB, j, 2)};
-                    const double* E[3] = {gb + 2, gb + 2 + G1B, gb + 2 + 2 * G1B};
-                    double f[3], dA[3], dB[3];
+                    const Real* E[3] = {gb + 2, gb + 2 + G1B, gb + 2 + 2 * G1B};
+                    Real f[3], dA[3], dB[3];
                     for (int x = 0; x < 3; ++x)
                     {
                         const int t = tt[x];
-                        f[x]  = (t <= ie[x] + je[x]) ? e1(E[x], LB, LAB, ie[x], je[x], t) : 0.0;
-                        dA[x] = 2.0 * aexp * e1(E[x], LB, LAB, ie[x] + 1, je[x], t) -
-                                (ie[x] > 0 ? ie[x] * e1(E[x], LB, LAB, ie[x] - 1, je[x], t) : 0.0);
-                        dB[x] = 2.0 * bexp * e1(E[x], LB, LAB, ie[x], je[x] + 1, t) -
-                                (je[x] > 0 ? je[x] * e1(E[x], LB, LAB, ie[x], je[x] - 1, t) : 0.0);
+                        f[x]  = (t <= ie[x] + je[x]) ? e1(E[x], LB, LAB, ie[x], je[x], t) : Real(0);
+                        dA[x] = Real(2) * aexp * e1(E[x], LB, LAB, ie[x] + 1, je[x], t) -
+                                (ie[x] > 0 ? ie[x] * e1(E[x], LB, LAB, ie[x] - 1, je[x], t) : Real(0));
+                        dB[x] = Real(2) * bexp * e1(E[x], LB, LAB, ie[x], je[x] + 1, t) -
+                                (je[x] > 0 ? je[x] * e1(E[x], LB, LAB, ie[x], je[x] - 1, t) : Real(0));
                     }
                     gA[0] += y * dA[0] * f[1] * f[2];
                     gA[1] += y * f[0] * dA[1] * f[2];
@@ -264,9 +282,9 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                 for (int e = lane; e < NCD * HCD1; e += GS)
                 {
                     const int kl = e / HCD1, h = e % HCD1;
-                    double hv = 0.0;
+                    Real hv = Real(0);
                     for (int ij = 0; ij < NAB; ++ij) hv += Gam[ij * NCD + kl] * Xs[ij * HCD1 + h];
-                    if (hv == 0.0)
+                    if (hv == Real(0))
                         continue;
                     const int tuv = tabs->htuv[LCD + 1][h];
                     const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
@@ -275,14 +293,14 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     const int k = kl / ND, l = kl % ND;
                     const int ke[3] = {cart_exp(LC, k, 0), cart_exp(LC, k, 1), cart_exp(LC, k, 2)};
                     const int le[3] = {cart_exp(LD, l, 0), cart_exp(LD, l, 1), cart_exp(LD, l, 2)};
-                    const double* E[3] = {gk + 2, gk + 2 + G1K, gk + 2 + 2 * G1K};
-                    double f[3], dC[3];
+                    const Real* E[3] = {gk + 2, gk + 2 + G1K, gk + 2 + 2 * G1K};
+                    Real f[3], dC[3];
                     for (int x = 0; x < 3; ++x)
                     {
                         const int t = tt[x];
-                        f[x]  = (t <= ke[x] + le[x]) ? e1(E[x], LD, LCD, ke[x], le[x], t) : 0.0;
-                        dC[x] = 2.0 * cexp * e1(E[x], LD, LCD, ke[x] + 1, le[x], t) -
-                                (ke[x] > 0 ? ke[x] * e1(E[x], LD, LCD, ke[x] - 1, le[x], t) : 0.0);
+                        f[x]  = (t <= ke[x] + le[x]) ? e1(E[x], LD, LCD, ke[x], le[x], t) : Real(0);
+                        dC[x] = Real(2) * cexp * e1(E[x], LD, LCD, ke[x] + 1, le[x], t) -
+                                (ke[x] > 0 ? ke[x] * e1(E[x], LD, LCD, ke[x] - 1, le[x], t) : Real(0));
                     }
                     gC[0] += hv * dC[0] * f[1] * f[2];
                     gC[1] += hv * f[0] * dC[1] * f[2];
@@ -304,10 +322,10 @@ __global__ void __launch_bounds__(32 * kGradWarps)
             const int tc = v.shell_atom[ket.sh1], td = v.shell_atom[ket.sh2];
             for (int x = 0; x < 3; ++x)
             {
-                atomicAdd(v.grad + 3 * ta + x, gA[x]);
-                atomicAdd(v.grad + 3 * tb + x, gB[x]);
-                atomicAdd(v.grad + 3 * tc + x, gC[x]);
-                atomicAdd(v.grad + 3 * td + x, -(gA[x] + gB[x] + gC[x]));
+                atomicAdd(v.grad + 3 * ta + x, widen(gA[x]));
+                atomicAdd(v.grad + 3 * tb + x, widen(gB[x]));
+                atomicAdd(v.grad + 3 * tc + x, widen(gC[x]));
+                atomicAdd(v.grad + 3 * td + x, widen(-(gA[x] + gB[x] + gC[x])));
             }
         }
         __syncwarp(gmask);

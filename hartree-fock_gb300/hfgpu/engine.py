@@ -66,7 +66,8 @@ class ScfOptions(ctypes.Structure):
 class GradRequest(ctypes.Structure):
     _fields_ = [("natom", ctypes.c_int), ("Z", ctypes.POINTER(ctypes.c_int)), ("xyz", ctypes.POINTER(ctypes.c_double)),
                 ("unrestricted", ctypes.c_int), ("D_alpha", ctypes.c_void_p), ("D_beta", ctypes.c_void_p),
-                ("W", ctypes.c_void_p), ("schwartz_threshold", ctypes.c_double), ("density_threshold", ctypes.c_double)]
+                ("W", ctypes.c_void_p), ("schwartz_threshold", ctypes.c_double), ("density_threshold", ctypes.c_double),
+                ("precision", ctypes.c_int), ("fp32_cutoff", ctypes.c_double)]
 
 
 class ScfResult(ctypes.Structure):
@@ -288,15 +289,17 @@ class Engine:
                                          _dp(X), charge, multiplicity, _dp(Da), _dp(Db)))
         return Da, Db
 
-    def gradient(self, Z, xyz, Da=None, Db=None, W=None, unrestricted=False, sthr=1e-10, dthr=1e-10):
+    def gradient(self, Z, xyz, Da=None, Db=None, W=None, unrestricted=False, sthr=1e-10, dthr=1e-10,
+                 precision=FP64, fp32_cutoff=1e-4):
         """Nuclear gradient (natom x 3, Eh/bohr) and the two-electron device time in ms.  With Da None the
-        densities of this engine's last scf() are used (the backward half of scf())."""
+        densities of this engine's last scf() are used (the backward half of scf()).  precision MIXED runs
+        the small-bound quartets' derivative integrals in FP32."""
         Zc = np.ascontiguousarray(Z, dtype=np.int32)
         X = np.ascontiguousarray(xyz, dtype=np.float64)
         arrs = [np.asfortranarray(m, dtype=np.float64) if m is not None else None for m in (Da, Db, W)]
         ptr = lambda m: m.ctypes.data if m is not None else None
         req = GradRequest(len(Zc), Zc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(X), 1 if unrestricted else 0,
-                          *[ptr(m) for m in arrs], sthr, dthr)
+                          *[ptr(m) for m in arrs], sthr, dthr, precision, fp32_cutoff)
         g = np.zeros((len(Zc), 3))
         ms = ctypes.c_double()
         self._check(lib().hfg_gradient(self.h, ctypes.byref(req), _dp(g), ctypes.byref(ms)))

@@ -259,6 +259,9 @@ typedef struct hfg_gradient_request
     const double* W;       /* host: total energy-weighted density sum_s C_occ eps_occ C_occ^T */
     double schwartz_threshold;
     double density_threshold;
+    int precision;      /* HFG_PRECISION_FP64, or HFG_PRECISION_MIXED: quartets whose bound Q_ab Q_cd max|D|
+                           is below fp32_cutoff run in FP32 (FP64 accumulation), as in the Fock build */
+    double fp32_cutoff;
 } hfg_gradient_request;
 
 int hfg_gradient(hfg_engine* engine, const hfg_gradient_request* req, double* grad, double* ms_two_electron);
