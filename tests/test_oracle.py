@@ -85,3 +85,31 @@ def test_oracle_survivors_are_the_reference_predicate(port):
             continue
         want.append((a, b, c, d))
     assert sorted(map(tuple, surv.tolist())) == want
+
+
+def test_oracle_jk_against_dense_einsum(port):
+    """The oracle's direct build (the reference's screening loop and digestion) against J and K contracted
+    densely from the full ERI tensor, H2O/6-31G with screening off.  The shell blocks carry the
+    reference's zero pattern (AO quartets it leaves to symmetry), so each element of the dense tensor is
+    taken from whichever of its 8 symmetric images the blocks define."""
+    import numpy as np
+
+    g = load_golden("h2o_631g")
+    B = port.Basis(g["soa"])
+    n, ns = B.nao, B.nshells
+    off = np.concatenate([[0], np.cumsum([B.nao_of(s) for s in range(ns)])])
+    T = np.zeros((n, n, n, n))
+    for a in range(ns):
+        for b in range(ns):
+            for c in range(ns):
+                for d in range(ns):
+                    T[off[a]:off[a + 1], off[b]:off[b + 1], off[c]:off[c + 1], off[d]:off[d + 1]] = B.eri(a, b, c, d)
+    imgs = np.stack([T.transpose(p) for p in ((0, 1, 2, 3), (1, 0, 2, 3), (0, 1, 3, 2), (1, 0, 3, 2),
+                                              (2, 3, 0, 1), (3, 2, 0, 1), (2, 3, 1, 0), (3, 2, 1, 0))])
+    pick = np.abs(imgs).argmax(axis=0)
+    T = np.take_along_axis(imgs, pick[None], axis=0)[0]
+    Da = g["Da"]
+    Dt = Da + g["Db"]
+    J, Ka, _, _ = B.fock_direct(B.schwartz(), Dt, Da, sthr=0.0, dthr=0.0)
+    assert np.max(np.abs(J - np.einsum("ijkl,kl->ij", T, Dt))) <= 1e-11
+    assert np.max(np.abs(Ka - np.einsum("ikjl,kl->ij", T, Da))) <= 1e-11
