@@ -41,6 +41,13 @@ constexpr unsigned form_mask(bool fp32)
     return (warp_form(fp32) ? (1u << kFormWarp) : (1u << kFormThread)) | (kGroup ? (1u << kFormGroup) : 0u);
 }
 
+// Resident blocks per SM a grid may take: the occupancy limit times the share, at least one.
+inline unsigned long long resident(int per_sm, float share)
+{
+    const int r = static_cast<int>(static_cast<float>(per_sm > 0 ? per_sm : 1) * share);
+    return static_cast<unsigned long long>(r > 0 ? r : 1);
+}
+
 template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
 {
     constexpr bool kWarpForm = warp_form(sizeof(Real) == 4);
@@ -64,7 +71,7 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
             if (e != cudaSuccess)
                 return e;
             const unsigned long long need = (c.count_host + 127) / 128; // 4 warps x 32-quartet windows
-            const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+            const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
             kern<<<static_cast<unsigned>(need < cap ? need : cap), 128, smem, c.stream>>>(
                 c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
             return cudaGetLastError();
@@ -83,7 +90,7 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
         if (e != cudaSuccess)
             return e;
         const unsigned long long need = (c.count_host + kWarpKernelWarps - 1) / kWarpKernelWarps;
-        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
         const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
         kern<<<grid, 32 * kWarpKernelWarps, smem, c.stream>>>(c.list, c.count_dev, c.view,
                                                               static_cast<const Real*>(c.boys_slice), c.tables);
@@ -100,7 +107,7 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
         if (e != cudaSuccess)
             return e;
         const unsigned long long need = (c.count_host + 127) / 128;
-        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
         const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
         kern<<<grid, 128, smem, c.stream>>>(c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
     }

@@ -25,6 +25,7 @@ struct ClassLaunch
     cudaStream_t stream;
     int num_sms;
     int form; // 0: the class's default form, else one of kFormThread / kFormWarp / kFormGroup
+    float share = 1.f; // fraction of the resident blocks per SM the grid may take (concurrent precisions)
 };
 // Kernel forms of a class kernel (eri_jk.cuh, eri_warp.cuh, eri_group.cuh).
 constexpr int kFormThread = 1, kFormWarp = 2, kFormGroup = 3;

@@ -41,13 +41,14 @@ class Stats(ctypes.Structure):
                                        "ms_eri_fp32")] + [("kernel_launches", ctypes.c_int),
                                                           ("form_fp64", ctypes.c_int * NUM_CLASSES),
                                                           ("form_fp32", ctypes.c_int * NUM_CLASSES),
-                                                          ("ms_tune", ctypes.c_double)]
+                                                          ("ms_tune", ctypes.c_double),
+                                                          ("ms_eri_both", ctypes.c_double)]
 
     def as_dict(self):
         d = {n: list(getattr(self, n)) for n in ("quartets_fp64", "quartets_fp32", "prim_quartets_fp64",
                                                  "prim_quartets_fp32", "form_fp64", "form_fp32")}
         d.update({n: getattr(self, n) for n in ("flops_fp64", "flops_fp32", "ms_total", "ms_lists", "ms_eri_fp64",
-                                                "ms_eri_fp32", "kernel_launches", "ms_tune")})
+                                                "ms_eri_fp32", "kernel_launches", "ms_tune", "ms_eri_both")})
         return d
 
 
@@ -105,6 +106,7 @@ def lib():
         L.hfg_set_kernel_form.argtypes = [vp, ip, ip, ip]
         L.hfg_set_primitive_threshold.argtypes = [vp, ctypes.c_double]
         L.hfg_set_graph_mode.argtypes = [vp, ip]
+        L.hfg_set_precision_overlap.argtypes = [vp, ip, ctypes.c_double]
         L.hfg_kernel_forms.argtypes = [vp, ip, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)]
         L.hfg_stream.argtypes = [vp]
         L.hfg_stream.restype = vp
@@ -232,6 +234,11 @@ class Engine:
         st = Stats()
         self._check(lib().hfg_fock_direct(self.h, ctypes.byref(req), ctypes.byref(st)))
         return st.as_dict()
+
+    def set_precision_overlap(self, on: bool, share: float = 1.0):
+        """Run a mixed build's FP32 class kernels concurrently with the FP64 ones (grids at `share` of the
+        resident blocks per SM)."""
+        self._check(lib().hfg_set_precision_overlap(self.h, 1 if on else 0, float(share)))
 
     def set_graph_mode(self, on: bool):
         """Replay device-pointer Fock builds as CUDA graphs (captured on first use per request key)."""

@@ -94,6 +94,8 @@ typedef struct hfg_fock_stats
     int form_fp64[HFG_NUM_CLASSES]; /* kernel form each class ran in (HFG_FORM_*; 0 = class not launched) */
     int form_fp32[HFG_NUM_CLASSES];
     double ms_tune;     /* host wall time spent timing kernel forms in this call (first use of a class only) */
+    double ms_eri_both; /* mixed builds with overlapped precisions: the span of all class kernels (FP64 and FP32
+                           run concurrently, so ms_eri_fp64 and ms_eri_fp32 overlap); 0 otherwise */
 } hfg_fock_stats;
 
 /* IntegralEngine::IntegralEngine(const BasisSet&) (include/IntegralEngine.hpp:11).  Packs the basis
@@ -143,6 +145,12 @@ int hfg_fock_direct(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_st
  * kernels).  HFG_FORM_AUTO forgets earlier timings; a form the class was not compiled in returns
  * HFG_ERR_UNSUPPORTED (with qclass -1 such classes keep AUTO). */
 int hfg_set_kernel_form(hfg_engine* engine, int qclass, int fp32, int form);
+/* Mixed builds run the FP32 class kernels on a second stream concurrently with the FP64 ones, each grid
+ * limited to `share` (0 < share <= 1) of the resident blocks per SM, so that the FP64-pipe bound and
+ * the FP32 / memory-latency bound kernels share the SMs.  On by default with share 1 (full grids).  No
+ * reference counterpart. */
+int hfg_set_precision_overlap(hfg_engine* engine, int on, double share);
+
 /* CUDA-graph replay of Fock builds (no reference counterpart; the SCF driver calls hfg_fock_direct on
  * device pointers every iteration).  On: a device-pointer request runs eagerly once and is captured
  * with every class kernel at a fixed grid (the kernels read their list lengths on the device); later
