@@ -33,7 +33,6 @@ constexpr bool warp_form(bool fp32)
 {
     return fp32 ? (QC == 14 || QC >= 17) : (QC == 12 || QC == 13 || QC == 14 || QC >= 16);
 }
-constexpr bool kWarp = warp_form(false);
 // The primitive-parallel group form exists for the small, contracted classes (L <= 3, <= 27 integrals).
 constexpr bool kGroup = (L <= 3) && (NAB * NCD <= 27);
 constexpr unsigned form_mask(bool fp32)
@@ -125,7 +124,6 @@ cudaError_t HFG_CAT(launch_class_, HFG_QCLASS)(const ClassLaunch& c)
     return c.uhf ? launch_t<double, true>(c) : launch_t<double, false>(c);
 }
 
-bool HFG_CAT(class_uses_warp_, HFG_QCLASS)() { return kWarp; }
 unsigned HFG_CAT(class_form_mask_, HFG_QCLASS)(bool fp32)
 {
     return form_mask(fp32) | (static_cast<unsigned>(warp_form(fp32) ? kFormWarp : kFormThread) << 16);

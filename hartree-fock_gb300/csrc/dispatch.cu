@@ -7,8 +7,7 @@ namespace hfg
 #define HFG_DECL(c)                                                                                                    \
     cudaError_t launch_class_##c(const ClassLaunch&);                                                                 \
     cudaError_t launch_grad_##c(const GradLaunch&);                                                                   \
-    unsigned class_form_mask_##c(bool);                                                                              \
-    bool class_uses_warp_##c();
+    unsigned class_form_mask_##c(bool);
 HFG_DECL(0) HFG_DECL(1) HFG_DECL(2) HFG_DECL(3) HFG_DECL(4) HFG_DECL(5) HFG_DECL(6) HFG_DECL(7) HFG_DECL(8)
 HFG_DECL(9) HFG_DECL(10) HFG_DECL(11) HFG_DECL(12) HFG_DECL(13) HFG_DECL(14) HFG_DECL(15) HFG_DECL(16)
 HFG_DECL(17) HFG_DECL(18) HFG_DECL(19) HFG_DECL(20)
@@ -19,12 +18,6 @@ static const ClassLauncher kLaunch[kNumQuartetClasses] = {
     launch_class_6,  launch_class_7,  launch_class_8,  launch_class_9,  launch_class_10, launch_class_11,
     launch_class_12, launch_class_13, launch_class_14, launch_class_15, launch_class_16, launch_class_17,
     launch_class_18, launch_class_19, launch_class_20};
-static bool (*const kWarp[kNumQuartetClasses])() = {
-    class_uses_warp_0,  class_uses_warp_1,  class_uses_warp_2,  class_uses_warp_3,  class_uses_warp_4,
-    class_uses_warp_5,  class_uses_warp_6,  class_uses_warp_7,  class_uses_warp_8,  class_uses_warp_9,
-    class_uses_warp_10, class_uses_warp_11, class_uses_warp_12, class_uses_warp_13, class_uses_warp_14,
-    class_uses_warp_15, class_uses_warp_16, class_uses_warp_17, class_uses_warp_18, class_uses_warp_19,
-    class_uses_warp_20};
 
 static const decltype(&launch_grad_0) kGrad[kNumQuartetClasses] = {
     launch_grad_0,  launch_grad_1,  launch_grad_2,  launch_grad_3,  launch_grad_4,  launch_grad_5,  launch_grad_6,
@@ -63,5 +56,4 @@ int class_default_form(int qclass, bool fp32)
     return (qclass >= 0 && qclass < kNumQuartetClasses) ? static_cast<int>((kMask[qclass](fp32) >> 16) & 0xffu) : 0;
 }
 
-bool class_uses_warp_kernel(int qclass) { return qclass >= 0 && qclass < kNumQuartetClasses && kWarp[qclass](); }
 } // namespace hfg

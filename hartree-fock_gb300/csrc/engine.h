@@ -32,7 +32,6 @@ constexpr int kFormThread = 1, kFormWarp = 2, kFormGroup = 3;
 using ClassLauncher = cudaError_t (*)(const ClassLaunch&);
 // Defined in classes.cu (one translation unit per quartet class).
 cudaError_t launch_class(int qclass, const ClassLaunch& L);
-bool class_uses_warp_kernel(int qclass);
 // Bit f set: form f is compiled for this class and precision.
 unsigned class_form_mask(int qclass, bool fp32);
 // The form a launch with form == 0 runs.

@@ -523,36 +523,4 @@ __global__ void __launch_bounds__(128) jk_class_kernel(const Quartet* __restrict
     }
 }
 
-// Schwartz bound of every pair of one pair class: Q = sqrt(max_ij (ij|ij)) (IntegralEngine.cpp:695-728).
-template <int LA, int LB>
-__global__ void __launch_bounds__(128) schwartz_kernel(const int* __restrict__ pair_ids, int npairs, FockView v,
-                                                       const double* __restrict__ boys_slice, double* __restrict__ Q)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    double* slice = reinterpret_cast<double*>(smem_raw);
-    stage_boys<double>(boys_slice, slice);
-    constexpr int NAB = ncart(LA) * ncart(LB);
-    const double* tb  = static_cast<const double*>(v.pptab[pair_class(LA, LB)]);
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x)
-    {
-        const int pid     = pair_ids[k];
-        const PairRec pr  = v.pairs[pid];
-        double acc[NAB * NAB];
-        eval_quartet<LA, LB, LA, LB, double>(pr, pr, tb, tb, slice, acc);
-        double mx = 0.0;
-        static_for<0, ncart(LA)>(
-            [&](auto I)
-            {
-                static_for<0, ncart(LB)>(
-                    [&](auto Jx)
-                    {
-                        constexpr int i = decltype(I)::value, j = decltype(Jx)::value;
-                        constexpr double an = ang_norm(LA, i) * ang_norm(LB, j);
-                        const double val    = acc[(i * ncart(LB) + j) * NAB + i * ncart(LB) + j] * (an * an);
-                        mx                  = fmax(mx, val);
-                    });
-            });
-        Q[pid] = sqrt(mx);
-    }
-}
 } // namespace hfg
