@@ -35,9 +35,13 @@ constexpr bool warp_form(bool fp32)
 }
 // The primitive-parallel group form exists for the small, contracted classes (L <= 3, <= 27 integrals).
 constexpr bool kGroup = (L <= 3) && (NAB * NCD <= 27);
+// FP32 classes whose thread form sits at the 255-register limit ((dp|ps), (dp|pp), (dp|ds), (dd|ps): one or
+// two blocks per SM) also compile the warp form, and the autotuner times both.
+constexpr bool dual_form(bool fp32) { return fp32 && (QC == 11 || QC == 12 || QC == 13 || QC == 16); }
 constexpr unsigned form_mask(bool fp32)
 {
-    return (warp_form(fp32) ? (1u << kFormWarp) : (1u << kFormThread)) | (kGroup ? (1u << kFormGroup) : 0u);
+    return (warp_form(fp32) || dual_form(fp32) ? (1u << kFormWarp) : 0u) |
+           (!warp_form(fp32) || dual_form(fp32) ? (1u << kFormThread) : 0u) | (kGroup ? (1u << kFormGroup) : 0u);
 }
 
 // Resident blocks per SM a grid may take: the occupancy limit times the share, at least one.
@@ -76,41 +80,51 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
             return cudaGetLastError();
         }
     }
-    if constexpr (kWarpForm)
+    constexpr bool kHasWarp = kWarpForm || dual_form(sizeof(Real) == 4);
+    constexpr bool kHasThread = !kWarpForm || dual_form(sizeof(Real) == 4);
+    if constexpr (kHasWarp)
     {
-        using W             = WarpLayout<LA, LB, LC, LD, Real>;
-        const size_t smem   = slice_bytes + sizeof(Real) * W::kPerWarp * kWarpKernelWarps;
-        auto kern           = jk_class_warp_kernel<LA, LB, LC, LD, Real, UHF>;
-        cudaError_t e       = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess)
-            return e;
-        int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kWarpKernelWarps, smem);
-        if (e != cudaSuccess)
-            return e;
-        const unsigned long long need = (c.count_host + kWarpKernelWarps - 1) / kWarpKernelWarps;
-        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
-        const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
-        kern<<<grid, 32 * kWarpKernelWarps, smem, c.stream>>>(c.list, c.count_dev, c.view,
-                                                              static_cast<const Real*>(c.boys_slice), c.tables);
+        if (form == kFormWarp)
+        {
+            using W             = WarpLayout<LA, LB, LC, LD, Real>;
+            const size_t smem   = slice_bytes + sizeof(Real) * W::kPerWarp * kWarpKernelWarps;
+            auto kern           = jk_class_warp_kernel<LA, LB, LC, LD, Real, UHF>;
+            cudaError_t e       = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess)
+                return e;
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kWarpKernelWarps, smem);
+            if (e != cudaSuccess)
+                return e;
+            const unsigned long long need = (c.count_host + kWarpKernelWarps - 1) / kWarpKernelWarps;
+            const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
+            const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
+            kern<<<grid, 32 * kWarpKernelWarps, smem, c.stream>>>(c.list, c.count_dev, c.view,
+                                                                  static_cast<const Real*>(c.boys_slice), c.tables);
+            return cudaGetLastError();
+        }
     }
-    else
+    if constexpr (kHasThread)
     {
-        auto kern           = jk_class_kernel<LA, LB, LC, LD, Real, UHF>;
-        const size_t smem   = slice_bytes;
-        cudaError_t e       = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess)
-            return e;
-        int per_sm = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
-        if (e != cudaSuccess)
-            return e;
-        const unsigned long long need = (c.count_host + 127) / 128;
-        const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
-        const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
-        kern<<<grid, 128, smem, c.stream>>>(c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
+        if (form == kFormThread)
+        {
+            auto kern           = jk_class_kernel<LA, LB, LC, LD, Real, UHF>;
+            const size_t smem   = slice_bytes;
+            cudaError_t e       = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess)
+                return e;
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+            if (e != cudaSuccess)
+                return e;
+            const unsigned long long need = (c.count_host + 127) / 128;
+            const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
+            const unsigned grid           = static_cast<unsigned>(need < cap ? need : cap);
+            kern<<<grid, 128, smem, c.stream>>>(c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
+            return cudaGetLastError();
+        }
     }
-    return cudaGetLastError();
+    return cudaErrorInvalidValue;
 }
 } // namespace
 
