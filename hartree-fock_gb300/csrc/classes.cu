@@ -1,11 +1,16 @@
-// Kernel instantiations and launcher of ONE shell-quartet class.  The build compiles this file once
-// per class with -DHFG_QCLASS=<0..20>, so the 21 classes compile in parallel.
+// Kernel instantiations and launchers of ONE shell-quartet class.  The build compiles this file three
+// times per class, -DHFG_QCLASS=<0..20> -DHFG_PART=<0..2>: part 0 the FP64 Fock kernels (and the form
+// mask), part 1 the FP32 Fock kernels, part 2 the gradient kernels, so that the 63 units compile in
+// parallel and the largest class does not serialise the build.
 #include "engine.h"
 #include "eri_grad.cuh"
 #include "eri_group.cuh"
 
 #ifndef HFG_QCLASS
 #error "compile with -DHFG_QCLASS=<quartet class>"
+#endif
+#ifndef HFG_PART
+#error "compile with -DHFG_PART=<0: FP64 Fock kernels, 1: FP32 Fock kernels, 2: gradient kernels>"
 #endif
 
 namespace hfg
@@ -131,10 +136,9 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
 #define HFG_CAT2(a, b) a##b
 #define HFG_CAT(a, b) HFG_CAT2(a, b)
 
-cudaError_t HFG_CAT(launch_class_, HFG_QCLASS)(const ClassLaunch& c)
+#if HFG_PART == 0
+cudaError_t HFG_CAT(launch_class64_, HFG_QCLASS)(const ClassLaunch& c)
 {
-    if (c.fp32)
-        return c.uhf ? launch_t<float, true>(c) : launch_t<float, false>(c);
     return c.uhf ? launch_t<double, true>(c) : launch_t<double, false>(c);
 }
 
@@ -142,7 +146,12 @@ unsigned HFG_CAT(class_form_mask_, HFG_QCLASS)(bool fp32)
 {
     return form_mask(fp32) | (static_cast<unsigned>(warp_form(fp32) ? kFormWarp : kFormThread) << 16);
 }
-
+#elif HFG_PART == 1
+cudaError_t HFG_CAT(launch_class32_, HFG_QCLASS)(const ClassLaunch& c)
+{
+    return c.uhf ? launch_t<float, true>(c) : launch_t<float, false>(c);
+}
+#else
 namespace
 {
 template <typename Real> cudaError_t launch_grad_t(const GradLaunch& c)
@@ -172,4 +181,5 @@ cudaError_t HFG_CAT(launch_grad_, HFG_QCLASS)(const GradLaunch& c)
         return cudaSuccess;
     return c.fp32 ? launch_grad_t<float>(c) : launch_grad_t<double>(c);
 }
+#endif
 } // namespace hfg

@@ -5,7 +5,8 @@
 namespace hfg
 {
 #define HFG_DECL(c)                                                                                                    \
-    cudaError_t launch_class_##c(const ClassLaunch&);                                                                 \
+    cudaError_t launch_class64_##c(const ClassLaunch&);                                                               \
+    cudaError_t launch_class32_##c(const ClassLaunch&);                                                               \
     cudaError_t launch_grad_##c(const GradLaunch&);                                                                   \
     unsigned class_form_mask_##c(bool);
 HFG_DECL(0) HFG_DECL(1) HFG_DECL(2) HFG_DECL(3) HFG_DECL(4) HFG_DECL(5) HFG_DECL(6) HFG_DECL(7) HFG_DECL(8)
@@ -13,11 +14,16 @@ HFG_DECL(9) HFG_DECL(10) HFG_DECL(11) HFG_DECL(12) HFG_DECL(13) HFG_DECL(14) HFG
 HFG_DECL(17) HFG_DECL(18) HFG_DECL(19) HFG_DECL(20)
 #undef HFG_DECL
 
-static const ClassLauncher kLaunch[kNumQuartetClasses] = {
-    launch_class_0,  launch_class_1,  launch_class_2,  launch_class_3,  launch_class_4,  launch_class_5,
-    launch_class_6,  launch_class_7,  launch_class_8,  launch_class_9,  launch_class_10, launch_class_11,
-    launch_class_12, launch_class_13, launch_class_14, launch_class_15, launch_class_16, launch_class_17,
-    launch_class_18, launch_class_19, launch_class_20};
+static const ClassLauncher kLaunch64[kNumQuartetClasses] = {
+    launch_class64_0, launch_class64_1, launch_class64_2, launch_class64_3, launch_class64_4, launch_class64_5,
+    launch_class64_6, launch_class64_7, launch_class64_8, launch_class64_9, launch_class64_10, launch_class64_11,
+    launch_class64_12, launch_class64_13, launch_class64_14, launch_class64_15, launch_class64_16, launch_class64_17,
+    launch_class64_18, launch_class64_19, launch_class64_20};
+static const ClassLauncher kLaunch32[kNumQuartetClasses] = {
+    launch_class32_0, launch_class32_1, launch_class32_2, launch_class32_3, launch_class32_4, launch_class32_5,
+    launch_class32_6, launch_class32_7, launch_class32_8, launch_class32_9, launch_class32_10, launch_class32_11,
+    launch_class32_12, launch_class32_13, launch_class32_14, launch_class32_15, launch_class32_16, launch_class32_17,
+    launch_class32_18, launch_class32_19, launch_class32_20};
 
 static const decltype(&launch_grad_0) kGrad[kNumQuartetClasses] = {
     launch_grad_0,  launch_grad_1,  launch_grad_2,  launch_grad_3,  launch_grad_4,  launch_grad_5,  launch_grad_6,
@@ -35,7 +41,7 @@ cudaError_t launch_class(int qclass, const ClassLaunch& L)
 {
     if (qclass < 0 || qclass >= kNumQuartetClasses)
         return cudaErrorInvalidValue;
-    return kLaunch[qclass](L);
+    return L.fp32 ? kLaunch32[qclass](L) : kLaunch64[qclass](L);
 }
 
 static unsigned (*const kMask[kNumQuartetClasses])(bool) = {

@@ -57,8 +57,9 @@ def _units():
     units = []
     for c in range(NUM_CLASSES):
         src = os.path.join(CSRC, "classes.cu")
-        flags = NVCC_FLAGS + [f"-DHFG_QCLASS={c}"]
-        units.append(("nvcc", src, flags, f"class{c:02d}", hdrs))
+        for part in range(3):  # FP64 Fock kernels, FP32 Fock kernels, gradient kernels
+            flags = NVCC_FLAGS + [f"-DHFG_QCLASS={c}", f"-DHFG_PART={part}"]
+            units.append(("nvcc", src, flags, f"class{c:02d}p{part}", hdrs))
     for name in ("engine.cu", "dispatch.cu", "peak.cu"):
         units.append(("nvcc", os.path.join(CSRC, name), NVCC_FLAGS, name[:-3], hdrs))
     for name in sorted(os.listdir(CSRC)):
@@ -88,7 +89,7 @@ def build(verbose: bool = True, jobs: int | None = None) -> str:
     units = _units()
     jobs = jobs or max(1, min(len(units), os.cpu_count() or 4))
     # Longest first: the d-class units dominate the wall time.
-    order = sorted(units, key=lambda u: (u[3].startswith("class") and int(u[3][5:]) or 0), reverse=True)
+    order = sorted(units, key=lambda u: (u[3].startswith("class") and int(u[3][5:7]) or 0), reverse=True)
     with cf.ThreadPoolExecutor(jobs) as ex:
         results = list(ex.map(_compile, order))
     objs = [o for o, _ in results]
