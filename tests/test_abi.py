@@ -38,3 +38,25 @@ def test_create_rejects_bad_arguments_without_touching_a_gpu():
     assert L.hfg_fock_direct(None, None, None) == -1
     assert L.hfg_schwartz(None, None) == -1
     assert L.hfg_version().decode().startswith("hfgpu")
+
+
+def test_engine_entry_points_reject_a_null_engine():
+    """Every engine-level entry point returns HFG_ERR_INVALID (-1) for a null handle and never dereferences it."""
+    from hfgpu import engine
+
+    L = engine.lib()
+    forms = (ctypes.c_int * 21)()
+    masks = (ctypes.c_uint * 21)()
+    cnt = ctypes.c_longlong()
+    out = (ctypes.c_double * 16)()
+    assert L.hfg_set_kernel_form(None, 0, 0, 1) == -1
+    assert L.hfg_kernel_forms(None, 0, 0, forms, masks) == -1
+    assert L.hfg_set_graph_mode(None, 1) == -1
+    assert L.hfg_set_precision_overlap(None, 1, 1.0) == -1
+    assert L.hfg_set_primitive_threshold(None, 1e-15) == -1
+    assert L.hfg_set_schwartz(None, None) == -1
+    assert L.hfg_survivors(None, None, 0, ctypes.byref(cnt)) == -1
+    assert L.hfg_eri_block(None, 0, 0, 0, 0, out) == -1
+    assert L.hfg_eri_block_noalloc(None, 0, 0, 0, 0, out) == -1
+    assert L.hfg_gradient(None, None, out, None) == -1
+    L.hfg_destroy(None)  # a no-op
