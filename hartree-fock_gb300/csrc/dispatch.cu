@@ -1,4 +1,5 @@
-// Table of the per-class launchers (one translation unit per class, see classes.cu).
+// Tables of the per-class launchers (three translation units per class, see classes.cu): FP64 and FP32
+// Fock kernels, gradient kernels, and the compiled-form masks.
 #include "engine.h"
 #include "eri_grad.cuh"
 

@@ -2,19 +2,23 @@
 //
 // Reference counterparts (MalachiF1/Hartree-Fock):
 //   IntegralEngine::IntegralEngine          src/IntegralEngine.cpp:13-75    -> hfg_create / pack_molecules
-//   computePrimitivePairData/HermiteCoeffs  src/IntegralEngine.cpp:995-1079 -> build_pair_tables (once per engine)
+//   computePrimitivePairData/HermiteCoeffs  src/IntegralEngine.cpp:995-1079 -> pack_molecules (once per engine)
 //   schwartzScreeningMatrix                 src/IntegralEngine.cpp:695-728  -> compute_schwartz
 //   SCF::buildFockMatrixDirect              src/SCF.cpp:523-744             -> fock_direct
 //
 // Device data layout (HBM):
-//   pairs_      PairRec per shell pair (a >= b within a molecule), oriented so l(sh1) >= l(sh2)
-//   pptab64_/32 per pair class, primitive-pair records of pp_stride(l1,l2) values: 1/p, p, P, Kw, E3
-//   cls_*       per pair class, pair ids sorted by (molecule, Q descending), with their Q values
-//   lists       per quartet class and precision, the surviving quartets (bra pair, ket pair)
+//   pairs       PairRec per shell pair (a >= b within a molecule), oriented so l(sh1) >= l(sh2), by pair
+//               id and, after the Schwartz sort, in sorted-list order (spairs; the lists hold those indices)
+//   pptab64/32  per pair class, primitive-pair records of pp_stride(l1,l2) values (p, P, W, 1/p, E3),
+//               renumbered in sorted order after the sort, and a field-major copy (ksoa) for the thread
+//               kernels' ket reads; primitive pairs below the screening bound are left out
+//   cls_*       per pair class, pair ids sorted by (molecule, primitive-pair count desc, Q desc), with
+//               their Q values and the segments of equal primitive-pair count
+//   lists       per quartet class and precision, the surviving quartets (bra, ket) as sorted indices
 //   matrices    per molecule n x n column-major blocks, concatenated (dD, X, Y, J, K)
-#include "engine.h"
-#include "eri_grad.cuh"
-#include "hfgpu.h"
+//
+// Streams: `stream` carries a build; mixed builds run the FP32 class kernels on stream2 concurrently with
+// the FP64 ones (fork after the list build, join before the symmetrisation).
 
 #include <algorithm>
 #include <array>
