@@ -19,6 +19,9 @@
 //
 // Streams: `stream` carries a build; mixed builds run the FP32 class kernels on stream2 concurrently with
 // the FP64 ones (fork after the list build, join before the symmetrisation).
+#include "engine.h"
+#include "eri_grad.cuh"
+#include "hfgpu.h"
 
 #include <algorithm>
 #include <array>
