@@ -72,7 +72,7 @@ def test_gradient_through_autograd_function():
     xyz = torch.tensor(g["xyz"], dtype=torch.float64, requires_grad=True)
     E = HFEnergy.apply(xyz)
     E.backward()
-    assert abs(float(E) - float(g["energy"])) <= 1e-8
+    assert abs(float(E.detach()) - float(g["energy"])) <= 1e-8
     assert np.max(np.abs(xyz.grad.numpy() - g["grad_fd"])) <= 1e-5
 
 
