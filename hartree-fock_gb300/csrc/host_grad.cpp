@@ -118,6 +118,10 @@ extern "C" int hfg_gradient_one_electron(const hfg_basis* b, const int* shell_at
                         PB[x] = P[x] - B[x];
                     }
                     const double K = std::exp(-aa * bb * ip * AB2);
+                    // K below 1e-30 contributes nothing representable (the derivative adds at most a factor
+                    // 2a to the bound of the one-electron integrals, which skip at the same K).
+                    if (K < 1e-30)
+                        continue;
                     Axis E[3];
                     for (int x = 0; x < 3; ++x) hermite_axis_g(la + 1, lb + 2, p, PA[x], PB[x], E[x]);
                     const double cprod = b->coeff[b->prim_off[sa] + pa] * b->coeff[b->prim_off[sb] + pb];

@@ -156,6 +156,12 @@ extern "C" int hfg_one_electron(const hfg_basis* b, int natom, const int* Z, con
                     PB[x] = P[x] - B[x];
                 }
                 const double K = std::exp(-aa * bb * ip * AB2);
+                // A primitive pair with K = exp(-ab/p |A-B|^2) below 1e-30 adds nothing representable to
+                // any S, T or V element: the remaining factors (contraction and normalisation, kinetic
+                // exponent powers, nuclear charges times Boys values) stay far below 1e16 for the s, p, d
+                // shells of the supported basis sets.
+                if (K < 1e-30)
+                    continue;
                 double E[3][kMaxL + 1][kE1][2 * kMaxL + 4];
                 for (int x = 0; x < 3; ++x) hermite_axis(la, lb + 2, p, PA[x], PB[x], E[x]);
                 const double cprod = b->coeff[b->prim_off[sa] + pa] * b->coeff[b->prim_off[sb] + pb];
