@@ -122,6 +122,7 @@ def lib():
         L.hfg_measure_fma_peak.argtypes = [ip, ip, dpp]
         L.hfg_measure_dmma_peak.argtypes = [ip, dpp]
         L.hfg_gradient.argtypes = [vp, ctypes.POINTER(GradRequest), dpp, dpp]
+        L.hfg_boys_eval.argtypes = [ip, ip, ip, ctypes.c_longlong, dpp, dpp]
         _lib = L
     return _lib
 
@@ -343,6 +344,16 @@ def measure_fma_peak(fp64: bool, device: int = 0) -> float:
     return t.value
 
 
+def boys_eval(m_max: int, T, fp32: bool = False, device: int = 0) -> np.ndarray:
+    """F_0(T) .. F_m_max(T) from the device Boys function of the ERI kernels; returns (len(T), m_max + 1)."""
+    T = np.ascontiguousarray(T, dtype=np.float64).ravel()
+    F = np.zeros((T.size, m_max + 1))
+    rc = lib().hfg_boys_eval(device, m_max, 1 if fp32 else 0, T.size, _dp(T), _dp(F))
+    if rc != HFG_OK:
+        raise HfgError(rc, "hfg_boys_eval failed")
+    return F
+
+
 def measure_dmma_peak(device: int = 0) -> float:
     """TFLOP/s of a register-only FP64 tensor-core (DMMA m8n8k4) loop on this GPU."""
     t = ctypes.c_double()
@@ -353,12 +364,19 @@ def measure_dmma_peak(device: int = 0) -> float:
 
 
 def run_input(text: str, precision: int = FP64, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0,
-              basis_dir: str | None = None, device: int = 0, graphs: bool = False):
+              basis_dir: str | None = None, device: int = 0, graphs: bool = False, input_frame: bool = False):
     """Runs a reference-format input end to end: parse, pack the basis, GPU direct SCF (graphs: replay
-    the Fock builds of the SCF iterations as CUDA graphs)."""
+    the Fock builds of the SCF iterations as CUDA graphs).
+
+    SYMMETRY TRUE (the reference's default) makes the reference move the molecule to its centre of mass
+    and rotate it into its point-group frame (src/Molecule.cpp:19-27) before anything is computed.  hfgpu
+    does not detect point groups, so such an input raises ValueError unless ``input_frame`` is True, which
+    runs the molecule as given: the energy is the same (it is invariant under rigid motions), densities
+    and gradients are in the input frame."""
     from . import basis as _basis, inputs as _inputs
 
     job = _inputs.parse(text)
+    _inputs.check_supported(job, input_frame)
     soa = _basis.pack(job.basis, job.Z, job.xyz, basis_dir)
     eng = Engine(soa, device=device)
     if graphs:

@@ -86,6 +86,20 @@ def parse(text: str) -> JobInput:
     return JobInput(charge, mult, Z, xyz, blocks["basis"][0], scf)
 
 
+def check_supported(job: JobInput, input_frame: bool = False) -> None:
+    """Rejects the keywords whose reference semantics this engine does not reproduce, instead of ignoring
+    them: SYMMETRY TRUE (the default; the reference translates to the centre of mass and rotates into the
+    point-group frame, src/Molecule.cpp:19-27) unless the caller accepts the input frame."""
+    if job.scf.get("symmetry", True) and not input_frame:
+        raise ValueError("SYMMETRY TRUE (the reference's default) reorients the molecule into its point-group "
+                         "frame (src/Molecule.cpp:19-27), which this engine does not do: set SYMMETRY FALSE in "
+                         "$scf, or run with input_frame=True to compute in the input frame (same energy; "
+                         "densities and gradients in the input frame)")
+    if not job.scf.get("direct", True):
+        raise ValueError("DIRECT FALSE (the reference's stored-integral SCF, src/SCF.cpp:233-521) is not "
+                         "available in this engine: set DIRECT TRUE")
+
+
 def scf_options(job: JobInput, precision: int = 0, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0) -> dict:
     """The hfg_scf_options fields for a parsed job, with the reference's defaults."""
     s = job.scf

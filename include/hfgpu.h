@@ -284,6 +284,11 @@ int hfg_measure_fma_peak(int device, int fp64, double* tflops);
 /* FP64 tensor-core (DMMA m8n8k4) throughput of this GPU in TFLOP/s (no reference counterpart). */
 int hfg_measure_dmma_peak(int device, double* tflops);
 
+/* The device Boys function of the ERI kernels, F_0(T) .. F_m_max(T) for n values of T (host arrays; F is
+ * n x (m_max + 1), row-major), evaluated on `device` by the same code the class kernels run (FP32 when
+ * fp32 != 0): a known-answer check of Boys::calculateBoys (src/Boys.cpp:14-71).  m_max <= 9, T >= 0. */
+int hfg_boys_eval(int device, int m_max, int fp32, long long n, const double* T, double* F);
+
 /* Library version string. */
 const char* hfg_version(void);
 

@@ -22,8 +22,10 @@ def load_golden(name):
     return d
 
 
-# Fock/SCF fixtures (the fd_* files hold finite-difference gradients and are loaded separately).
-GOLDEN_NAMES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("fd_"))
+# Fock/SCF fixtures of the small systems.  Loaded separately: fd_* (finite-difference gradients), cfg_*
+# (the benchmarked sizes, tests/test_gpu_configs.py) and boys_values (tests/test_gpu_boys.py).
+GOLDEN_NAMES = sorted(f[:-4] for f in os.listdir(GOLDEN)
+                      if f.endswith(".npz") and not f.startswith(("fd_", "cfg_", "boys_")))
 
 
 @pytest.fixture(scope="session")

@@ -23,7 +23,7 @@ from oracle import ref  # noqa: E402
 TIGHT = dict(ENERGY_TOL="1e-10", DENSITY_TOL="1e-7", DIIS_TOL="1e-7", MAX_ITER=100)
 
 SYSTEMS = {
-    # BASELINE config 0: the monomer, RHF/6-31G, DIIS size 6.
+    # The water monomer, RHF/6-31G, DIIS size 6 (the smallest benchmarked case).
     "h2o_631g": (w.monomer, "6-31G", 0, 1, dict(DIIS_SIZE=6)),
     # The reference README example: UHF with HOMO/LUMO mixing, here on the +1 doublet.
     "h2o_cation_uhf_631g": (w.monomer, "6-31G", 1, 2, dict(UNRESTRICTED=True, GUESS_MIX=2)),

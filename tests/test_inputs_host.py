@@ -41,6 +41,29 @@ def test_parse_rejects_unknown_keyword():
         inputs.parse("$molecule\n0 1\nH 0 0 0\n$end\n$scf\nFOO 1\n$end\n$basis\nsto-3g\n$end\n")
 
 
+_MIN = "$molecule\n0 1\nH 0 0 0\nH 0 0 1.4\n$end\n$scf\n{scf}$end\n$basis\nsto-3g\n$end\n"
+
+
+def test_symmetry_true_is_rejected_not_ignored():
+    """SYMMETRY TRUE (also the default) reorients the molecule in the reference (Molecule.cpp:19-27)."""
+    from hfgpu import inputs
+
+    for scf in ("", "SYMMETRY TRUE\n"):
+        job = inputs.parse(_MIN.format(scf=scf))
+        with pytest.raises(ValueError, match="SYMMETRY"):
+            inputs.check_supported(job)
+        inputs.check_supported(job, input_frame=True)  # accepted when the caller asks for the input frame
+    inputs.check_supported(inputs.parse(_MIN.format(scf="SYMMETRY FALSE\n")))
+
+
+def test_direct_false_is_rejected_not_ignored():
+    from hfgpu import inputs
+
+    job = inputs.parse(_MIN.format(scf="SYMMETRY FALSE\nDIRECT FALSE\n"))
+    with pytest.raises(ValueError, match="DIRECT"):
+        inputs.check_supported(job)
+
+
 @pytest.mark.parametrize("name", ["h2o_631g", "w2_631gss", "w2_ccpvdz"])
 def test_one_electron_matches_reference(name):
     from hfgpu import build, engine
