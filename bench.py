@@ -14,9 +14,14 @@ SCHWARTZ_THRESH = DENSITY_THRESH = 1e-10.  A step = one hfg_fock_direct call.
              builds' two-electron energies.
 * roofline   the dominant kernel group (the FP64 ERI class kernels), achieved algorithmic FP64 FLOP/s
              (engine work model) over their CUDA-event time, against the FP64 FMA peak this run measures.
-* cpu_baseline / --impl reference   the C restatement of the reference's OpenMP build (oracle/) timed
-             on this host on a seeded sample of bra shell pairs and scaled to the full build by the
-             number of surviving shell quartets.
+* scf        (N=1) full RHF SCFs of the workload, mixed and FP64 (wall time, iterations, |dE|), and the
+             mixed-precision nuclear gradient after the mixed SCF; --scf adds the UHF doublet and the FP64
+             gradient, --no-scf skips them.
+* cpu_baseline / --impl reference   the C restatement of the reference's OpenMP build (oracle/, built
+             with the reference's release flags) on this host's cores.  A CPU step is the build over a
+             seeded sample of bra shell pairs: its wall time is measured (ms_per_step) and its Fock builds/s
+             is the fraction of the build's surviving shell quartets it held over that time;
+             --cpu-full also times one unsampled build to check that scaling.
 
 Multi-GPU (torchrun): every rank builds the same workload on its own GPU (independent replicas, no
 collective on the data path; weak scaling).
@@ -54,7 +59,11 @@ def parse_args():
     ap.add_argument("--fp32-cutoff", type=float, default=1e-4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of one baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--scf", action="store_true", help="also time full SCFs (mixed and FP64)")
+    ap.add_argument("--scf", action="store_true",
+                    help="also time the UHF SCFs and the FP64 gradient (the RHF SCFs and the mixed gradient always run at N=1)")
+    ap.add_argument("--no-scf", action="store_true", help="skip the SCF and gradient timings")
+    ap.add_argument("--cpu-full", action="store_true",
+                    help="--impl reference: also time one full, unsampled CPU build (minutes) against the sampled estimate")
     ap.add_argument("--batch", action="store_true",
                     help="also time batched builds of 256 uneven (H2O)_k/6-31G chains (eager and CUDA-graph replay)")
     return ap.parse_args()
@@ -170,86 +179,117 @@ def make_workload(name):
     return Z, xyz, soa
 
 
-def cpu_baseline(soa, Z, xyz, Da, target_s: float, total_quartets: int | None = None, seed: int = 0):
-    """Time the oracle's OpenMP build on a seeded sample of bra shell pairs; scale to the full build."""
+def cpu_density(soa, Z, xyz):
+    """Core-Hamiltonian guess density of the workload on the CPU (the oracle's one-electron integrals and
+    numpy's FP64 eigensolver), for the CPU arms, which must not need the GPU."""
     import numpy as np
 
     from oracle import port
 
-    port.build()
     B = port.Basis(soa)
-    cores = port.lib().orc_num_threads()
-    Q = B.schwartz()
-    dt, da = 2.0 * Da, Da
-    if total_quartets is None:
-        total_quartets = int(B.count_survivors(Q, dt, da))
-    ns = B.nshells
-    npairs = ns * (ns + 1) // 2
-    rng = np.random.default_rng(seed)
+    S, T, V = B.one_electron(Z, xyz)
+    w, U = np.linalg.eigh(S)
+    X = (U * np.where(w > 0, 1.0 / np.sqrt(np.maximum(w, 1e-300)), 0.0)) @ U.T
+    _, Cp = np.linalg.eigh(X.T @ (T + V) @ X)
+    C = X @ Cp
+    nocc = sum(Z) // 2
+    return C[:, :nocc] @ C[:, :nocc].T
 
-    def run(frac):
-        mask = (rng.random(npairs) < frac).astype(np.uint8)
+
+class CpuBuild:
+    """The reference's direct Fock build on the host cores: the C restatement of SCF::buildFockMatrixDirect
+    (oracle/hf_oracle.c, OpenMP over all host threads) built with the reference's release flags.
+
+    One step runs the build over a seeded random sample of bra shell pairs (SCF.cpp's outer loop), so that a
+    step takes seconds instead of the minutes of a full build.  Its throughput in Fock builds/s is the
+    measured wall time of the step scaled by the fraction of the build's surviving shell quartets the
+    sample held; ``full()`` times one unsampled build for the check of that scaling."""
+
+    def __init__(self, soa, Z, xyz, Da, total_quartets=None):
+        from oracle import port
+
+        port.build()
+        self.B = port.Basis(soa, release=True)
+        self.cores = port.lib(True).orc_num_threads()
+        self.Q = self.B.schwartz()
+        self.dt, self.da = 2.0 * Da, Da
+        self.total = int(total_quartets if total_quartets is not None else self.B.count_survivors(self.Q, self.dt, self.da))
+        ns = self.B.nshells
+        self.npairs = ns * (ns + 1) // 2
+
+    def sample(self, frac, seed):
+        import numpy as np
+
+        mask = (np.random.default_rng(seed).random(self.npairs) < frac).astype(np.uint8)
         t0 = time.perf_counter()
-        _, _, _, n = B.fock_direct_sample(Q, dt, da, mask)
-        return time.perf_counter() - t0, int(n), int(mask.sum())
+        _, _, _, n = self.B.fock_direct_sample(self.Q, self.dt, self.da, mask)
+        t = time.perf_counter() - t0
+        return {"seconds": t, "quartets": int(n), "bra_pairs": int(mask.sum()), "fraction": n / max(self.total, 1),
+                "builds_per_s": (n / max(self.total, 1)) / t if t > 0 else 0.0}
 
-    frac = 2e-4
-    t, n, m = run(frac)
-    while t < 0.5 and frac < 0.5:  # calibrate to a measurable sample
-        frac *= 4
-        t, n, m = run(frac)
-    per_q = t / max(n, 1)
-    frac = min(1.0, frac * target_s / max(t, 1e-3))
-    t, n, m = run(frac)
-    est = t * total_quartets / max(n, 1)
-    return {"builds_per_s": 1.0 / est, "cores": cores, "sample_seconds": t, "sample_quartets": n,
-            "sample_bra_pairs": m, "total_quartets": total_quartets, "est_build_seconds": est,
-            "calibration_s_per_quartet": per_q}
+    def calibrate(self, target_s, seed=12345):
+        """Sampling fraction whose step takes about target_s seconds."""
+        frac = 2e-4
+        r = self.sample(frac, seed)
+        while r["seconds"] < 0.3 and frac < 0.5:
+            frac *= 4
+            r = self.sample(frac, seed)
+        return min(1.0, frac * target_s / max(r["seconds"], 1e-3))
+
+    def full(self):
+        t0 = time.perf_counter()
+        _, _, _, n = self.B.fock_direct(self.Q, self.dt, self.da)
+        t = time.perf_counter() - t0
+        return {"seconds": t, "quartets": int(n), "builds_per_s": 1.0 / t}
+
+
+def cpu_baseline(soa, Z, xyz, Da, target_s: float, total_quartets: int | None = None):
+    """A bounded CPU sample (about target_s seconds of work) for the GPU arm's cpu_baseline object."""
+    cb = CpuBuild(soa, Z, xyz, Da, total_quartets)
+    r = cb.sample(cb.calibrate(target_s), seed=0)
+    return {"value": r["builds_per_s"], "unit": "Fock builds/s", "cores": cb.cores, "kind": "port",
+            "sample": (f"{r['bra_pairs']} of {cb.npairs} bra shell pairs (seeded), {r['quartets']} of {cb.total} "
+                       f"surviving quartets ({100 * r['fraction']:.3f}% of the build) in {r['seconds']:.2f} s measured; "
+                       f"builds/s = sampled fraction / measured seconds"),
+            "build": "oracle/hf_oracle.c with the reference's release flags (Makefile:47, without -march=native/-flto)"}
 
 
 def reference_arm(args, dist):
-    """--impl reference: the reference algorithm (C restatement, OpenMP, all host cores) on this host."""
+    """--impl reference: the reference's direct Fock build on the host cores (CpuBuild), on this arm's
+    workload, metric and unit.  Every step is a bounded sample of the build whose wall time is measured;
+    ms_per_step is that measured time, and value the median over the steps of sampled fraction / time."""
     if dist.rank != 0:
         return
-    import numpy as np
-
-    from hfgpu import basis, workloads
-
     Z, xyz, soa = make_workload(args.workload)
-    # The core guess needs the GPU host path; the reference arm uses a density of the same structure
-    # built on the CPU: the oracle's one-electron integrals and numpy's eigensolver (FP64).
-    from oracle import port
-
-    port.build()
-    B = port.Basis(soa)
-    S, T, V = B.one_electron(Z, xyz)
-    h = T + V
-    w, U = np.linalg.eigh(S)
-    X = (U * np.where(w > 0, 1.0 / np.sqrt(np.maximum(w, 1e-300)), 0.0)) @ U.T
-    e, Cp = np.linalg.eigh(X.T @ h @ X)
-    C = X @ Cp
-    nocc = (sum(Z)) // 2
-    Da = C[:, :nocc] @ C[:, :nocc].T
-    samples = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline(soa, Z, xyz, Da, args.cpu_seconds / 2, seed=i)
-        if i >= args.warmup:
-            samples.append(r)
-    value = statistics.median(s["builds_per_s"] for s in samples)
-    r0 = samples[0]
-    sample = (f"seeded random {r0['sample_bra_pairs']} of {len(soa['l']) * (len(soa['l']) + 1) // 2} bra shell pairs "
-              f"({r0['sample_quartets']} of {r0['total_quartets']} surviving quartets, {r0['sample_seconds']:.1f} s), "
-              f"scaled by quartet count")
+    Da = cpu_density(soa, Z, xyz)
+    cb = CpuBuild(soa, Z, xyz, Da)
+    # Steps sized so that warm-up and timed steps take about --cpu-seconds x 12 in all (3 minutes by default).
+    per_step = min(8.0, max(0.5, 12.0 * args.cpu_seconds / max(1, args.steps + args.warmup)))
+    frac = cb.calibrate(per_step)
+    runs = [cb.sample(frac, seed=i) for i in range(args.warmup + args.steps)][args.warmup:]
+    value = statistics.median(r["builds_per_s"] for r in runs)
+    ms_step = statistics.median(1000.0 * r["seconds"] for r in runs)
     line = {
         "metric": METRIC, "value": value, "unit": "Fock builds/s", "impl": "reference", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded water lattice)",
-        "config": {"workload": WORKLOADS[args.workload]["name"], "precision": "fp64 (reference algorithm)"},
-        "cpu_baseline": {"value": value, "unit": "Fock builds/s", "cores": r0["cores"], "kind": "port",
-                         "sample": sample},
+        "config": {"workload": WORKLOADS[args.workload]["name"], "precision": "fp64 (reference algorithm)",
+                   "step": "the direct build over a seeded random sample of bra shell pairs"},
+        "sampling": {"fraction_of_build_per_step": statistics.median(r["fraction"] for r in runs),
+                     "quartets_per_step": int(statistics.median(r["quartets"] for r in runs)),
+                     "total_quartets": cb.total, "extrapolated_builds_per_s": value,
+                     "extrapolated_ms_per_full_build": 1000.0 / value if value else None},
+        "cpu_baseline": {"value": value, "unit": "Fock builds/s", "cores": cb.cores, "kind": "port",
+                         "sample": (f"{args.steps} steps of {100 * statistics.median(r['fraction'] for r in runs):.3f}% "
+                                    f"of the build's surviving quartets each ({ms_step / 1000:.2f} s median, measured)"),
+                         "build": "oracle/hf_oracle.c with the reference's release flags (Makefile:47, without "
+                                  "-march=native/-flto)"},
         "e2e": {"value": value, "unit": "Fock builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
+    if args.cpu_full:
+        line["full_build"] = cb.full()
+        line["full_build"]["sampled_estimate_error"] = value / line["full_build"]["builds_per_s"] - 1.0
     print(json.dumps(line), flush=True)
 
 
@@ -347,11 +387,7 @@ def gpu_arm(args, dist):
         cpu = None
         if not args.no_cpu_baseline:
             nq = sum(st["quartets_fp64"]) + sum(st["quartets_fp32"])
-            r = cpu_baseline(soa, Z, xyz, Da, args.cpu_seconds, total_quartets=nq)
-            cpu = {"value": r["builds_per_s"], "unit": "Fock builds/s", "cores": r["cores"], "kind": "port",
-                   "sample": (f"seeded random {r['sample_bra_pairs']} bra shell pairs, {r['sample_quartets']} of "
-                              f"{r['total_quartets']} surviving quartets in {r['sample_seconds']:.1f} s, scaled by "
-                              f"quartet count")}
+            cpu = cpu_baseline(soa, Z, xyz, Da, args.cpu_seconds, total_quartets=nq)
         out = {
             "metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -390,17 +426,17 @@ def gpu_arm(args, dist):
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }
-        if args.scf:
-            out["scf"] = scf_timings(soa, Z, xyz, dev, args.fp32_cutoff)
+        if not args.no_scf and dist.world == 1:
+            out["scf"] = scf_timings(soa, Z, xyz, dev, args.fp32_cutoff, full=args.scf)
         if args.batch:
             out["batched"] = batch_timings(dev, args.fp32_cutoff, args.steps, args.warmup)
     return out
 
 
-def scf_timings(soa, Z, xyz, dev, cutoff):
-    """Full SCFs of the workload: RHF in FP64 and mixed precision (the headline speed-up), the mixed-precision
-    nuclear gradient after the mixed SCFs (for RHF also the FP64 gradient on the same densities), and the
-    +1 doublet UHF (GUESS_MIX 2) in FP64 and mixed precision."""
+def scf_timings(soa, Z, xyz, dev, cutoff, full=False):
+    """Full SCFs of the workload: RHF in FP64 and mixed precision (the headline speed-up) and the
+    mixed-precision nuclear gradient after the mixed SCF; with ``full`` also the FP64 gradient on the same
+    densities and the +1 doublet UHF (GUESS_MIX 2) in FP64 and mixed precision."""
     import numpy as np
 
     from hfgpu.engine import FP64, MIXED, Engine
@@ -429,8 +465,9 @@ def scf_timings(soa, Z, xyz, dev, cutoff):
         eng.close()
         return out
 
-    res = {"rhf": {"fp64": one(FP64, 0, 1, False), "mixed": one(MIXED, 0, 1, "both")},
-           "uhf_cation_doublet": {"fp64": one(FP64, 1, 2, False), "mixed": one(MIXED, 1, 2, True)}}
+    res = {"rhf": {"fp64": one(FP64, 0, 1, False), "mixed": one(MIXED, 0, 1, "both" if full else True)}}
+    if full:
+        res["uhf_cation_doublet"] = {"fp64": one(FP64, 1, 2, False), "mixed": one(MIXED, 1, 2, True)}
     for k in res:
         res[k]["delta_e"] = abs(res[k]["mixed"]["e_total"] - res[k]["fp64"]["e_total"])
         res[k]["speedup"] = res[k]["fp64"]["seconds"] / res[k]["mixed"]["seconds"]

@@ -43,10 +43,20 @@ constexpr bool kGroup = (L <= 3) && (NAB * NCD <= 27);
 // FP32 classes whose thread form sits at the 255-register limit ((dp|ps), (dp|pp), (dp|ds), (dd|ps): one or
 // two blocks per SM) also compile the warp form, and the autotuner times both.
 constexpr bool dual_form(bool fp32) { return fp32 && (QC == 11 || QC == 12 || QC == 13 || QC == 16); }
+// Ket-chunked thread form (FP32 d classes): ket components per thread, chosen so that R, G[HAB][CH] and
+// ERI[NAB][CH] stay in registers (HL + (HAB + NAB) * CH floats well below 255); 0 = not compiled.
+//   (dp|pp) (dp|ds): 3   (dp|dp): 2   (dd|ps) (dd|pp) (dd|ds) (dd|dp): 1
+constexpr int chunk_width(bool fp32)
+{
+    if (!fp32)
+        return 0;
+    return (QC == 12 || QC == 13) ? 3 : QC == 14 ? 2 : (QC >= 16 && QC <= 19) ? 1 : 0;
+}
 constexpr unsigned form_mask(bool fp32)
 {
     return (warp_form(fp32) || dual_form(fp32) ? (1u << kFormWarp) : 0u) |
-           (!warp_form(fp32) || dual_form(fp32) ? (1u << kFormThread) : 0u) | (kGroup ? (1u << kFormGroup) : 0u);
+           (!warp_form(fp32) || dual_form(fp32) ? (1u << kFormThread) : 0u) | (kGroup ? (1u << kFormGroup) : 0u) |
+           (chunk_width(fp32) > 0 ? (1u << kFormChunk) : 0u);
 }
 
 // Resident blocks per SM a grid may take: the occupancy limit times the share, at least one.
@@ -82,6 +92,32 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
             const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
             kern<<<static_cast<unsigned>(need < cap ? need : cap), 128, smem, c.stream>>>(
                 c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
+            return cudaGetLastError();
+        }
+    }
+    constexpr int kChunk = chunk_width(sizeof(Real) == 4);
+    if constexpr (kChunk > 0)
+    {
+        if (form == kFormChunk)
+        {
+            constexpr int nch = num_chunks<LC, LD, kChunk>();
+            auto kern         = jk_class_chunk_kernel<LA, LB, LC, LD, Real, UHF, kChunk>;
+            const size_t smem = slice_bytes;
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess)
+                return e;
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+            if (e != cudaSuccess)
+                return e;
+            // Quartet blocks of 128; every one is NCH consecutive blocks (one per chunk).
+            const unsigned long long need = (c.count_host + 127) / 128;
+            unsigned long long cap = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share) / nch;
+            if (cap < 1)
+                cap = 1;
+            const unsigned long long qblocks = need < cap ? need : cap;
+            kern<<<static_cast<unsigned>(qblocks * nch), 128, smem, c.stream>>>(c.list, c.count_dev, c.view,
+                                                                                  static_cast<const Real*>(c.boys_slice));
             return cudaGetLastError();
         }
     }
@@ -140,6 +176,25 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
 cudaError_t HFG_CAT(launch_class64_, HFG_QCLASS)(const ClassLaunch& c)
 {
     return c.uhf ? launch_t<double, true>(c) : launch_t<double, false>(c);
+}
+
+cudaError_t HFG_CAT(launch_stored_, HFG_QCLASS)(const StoredLaunch& c)
+{
+    if (c.count == 0)
+        return cudaSuccess;
+    constexpr int nch = num_chunks<LC, LD, stored_chunk<LA, LB, LC, LD>()>();
+    auto kern = c.uhf ? jk_stored_kernel<LA, LB, LC, LD, true> : jk_stored_kernel<LA, LB, LC, LD, false>;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);
+    if (e != cudaSuccess)
+        return e;
+    const unsigned long long need = (c.count + 127) / 128;
+    unsigned long long cap = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1) / nch;
+    if (cap < 1)
+        cap = 1;
+    const unsigned long long qblocks = need < cap ? need : cap;
+    kern<<<static_cast<unsigned>(qblocks * nch), 128, 0, c.stream>>>(c.list, c.count, c.view, c.store);
+    return cudaGetLastError();
 }
 
 unsigned HFG_CAT(class_form_mask_, HFG_QCLASS)(bool fp32)

@@ -9,6 +9,7 @@ namespace hfg
     cudaError_t launch_class64_##c(const ClassLaunch&);                                                               \
     cudaError_t launch_class32_##c(const ClassLaunch&);                                                               \
     cudaError_t launch_grad_##c(const GradLaunch&);                                                                   \
+    cudaError_t launch_stored_##c(const StoredLaunch&);                                                               \
     unsigned class_form_mask_##c(bool);
 HFG_DECL(0) HFG_DECL(1) HFG_DECL(2) HFG_DECL(3) HFG_DECL(4) HFG_DECL(5) HFG_DECL(6) HFG_DECL(7) HFG_DECL(8)
 HFG_DECL(9) HFG_DECL(10) HFG_DECL(11) HFG_DECL(12) HFG_DECL(13) HFG_DECL(14) HFG_DECL(15) HFG_DECL(16)
@@ -30,6 +31,19 @@ static const decltype(&launch_grad_0) kGrad[kNumQuartetClasses] = {
     launch_grad_0,  launch_grad_1,  launch_grad_2,  launch_grad_3,  launch_grad_4,  launch_grad_5,  launch_grad_6,
     launch_grad_7,  launch_grad_8,  launch_grad_9,  launch_grad_10, launch_grad_11, launch_grad_12, launch_grad_13,
     launch_grad_14, launch_grad_15, launch_grad_16, launch_grad_17, launch_grad_18, launch_grad_19, launch_grad_20};
+
+static const decltype(&launch_stored_0) kStored[kNumQuartetClasses] = {
+    launch_stored_0,  launch_stored_1,  launch_stored_2,  launch_stored_3,  launch_stored_4,  launch_stored_5,
+    launch_stored_6,  launch_stored_7,  launch_stored_8,  launch_stored_9,  launch_stored_10, launch_stored_11,
+    launch_stored_12, launch_stored_13, launch_stored_14, launch_stored_15, launch_stored_16, launch_stored_17,
+    launch_stored_18, launch_stored_19, launch_stored_20};
+
+cudaError_t launch_stored(int qclass, const StoredLaunch& L)
+{
+    if (qclass < 0 || qclass >= kNumQuartetClasses)
+        return cudaErrorInvalidValue;
+    return kStored[qclass](L);
+}
 
 cudaError_t launch_grad(int qclass, const GradLaunch& L)
 {

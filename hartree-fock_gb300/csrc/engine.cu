@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -122,7 +123,8 @@ struct hfg_engine
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev2[4] {};
     bool overlap = true;
-    float overlap_share = 1.0f;
+    float overlap_share = 1.0f;   // FP64 class kernels' grids
+    float overlap_share32 = 1.0f; // FP32 class kernels' grids
     std::string last_error;
 
     int nmol = 0;
@@ -211,6 +213,12 @@ struct hfg_engine
     hfg::DevBuf<double> d_smax2;   // 2 * shell maxima of |dD_tot|
     hfg::DevBuf<double> d_store;
     hfg::DevBuf<hfg::Quartet> d_tmp_list;
+    // Stored integrals (hfg_store_integrals): per quartet class the Schwartz survivors (sorted pair
+    // indices) and their FP64 integral blocks, row-major [ij][kl] per quartet.
+    double conv_thr = -1.0;
+    unsigned long long conv_n[hfg::kNumQuartetClasses] {};
+    hfg::DevBuf<hfg::Quartet> d_conv_list[hfg::kNumQuartetClasses];
+    hfg::DevBuf<double> d_conv[hfg::kNumQuartetClasses];
     hfg::DevBuf<unsigned long long> d_tmp_count;
 
     // Kernel forms: the caller's setting per (class, precision), and the pick per (class, precision, UHF).
@@ -1366,7 +1374,7 @@ static int enqueue_build(hfg_engine* e, const hfg_fock_request& r, bool graph, i
             c.uhf        = uhf;
             c.stream     = ps;
             c.num_sms    = e->num_sms;
-            c.share      = overlap ? e->overlap_share : 1.f;
+            c.share      = overlap ? (prec == 1 ? e->overlap_share32 : e->overlap_share) : 1.f;
             if (graph)
             {
                 const int set  = e->form_set[qc][prec];
@@ -1559,6 +1567,154 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
     }
 }
 
+// Stored-integral path (the reference's conventional SCF): IntegralEngine::electronRepulsionTensor
+// (src/IntegralEngine.cpp:635-692) evaluates every shell quartet that survives Schwartz screening once;
+// here the survivors come from the list builder with the density test switched off (threshold 0 passes
+// every candidate), and each class list is evaluated in store mode into its own FP64 buffer.
+static void store_integrals(hfg_engine* e, double sthr, size_t* bytes_out)
+{
+    if (!(sthr >= 0.0) || !std::isfinite(sthr))
+        throw HfgError(HFG_ERR_INVALID, "store_integrals: threshold must be finite and >= 0");
+    if (!e->have_Q)
+    {
+        compute_schwartz(e);
+        sort_classes(e);
+    }
+    size_lists(e, sthr, false);
+    const long long N2 = e->mat_total;
+    for (int k = 0; k < 3; ++k)
+    {
+        e->d_dD[k].alloc(N2);
+        e->d_acc[k].alloc(N2);
+        e->d_out[k].alloc(N2);
+        e->d_smax[k].alloc(e->smax_total);
+        e->d_smaxf[k].alloc(e->smax_total);
+        HFG_CUDA(cudaMemsetAsync(e->d_dD[k].p, 0, sizeof(double) * N2, e->stream));
+    }
+    e->d_smax2.alloc(e->smax_total);
+    build_lists(e, false, false, sthr, 0.0, 0.0); // density threshold 0: Schwartz survivors only
+    size_t bytes = 0;
+    for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+    {
+        const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+        const int P2 = qc - P1 * (P1 + 1) / 2;
+        const size_t nq = ncart(pair_class_l1(P1)) * ncart(pair_class_l2(P1)) * ncart(pair_class_l1(P2)) * ncart(pair_class_l2(P2));
+        bytes += e->h_counts[2 * qc] * (nq * sizeof(double) + sizeof(Quartet));
+    }
+    size_t free_b = 0, total_b = 0;
+    HFG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (bytes > free_b / 10 * 8)
+        throw HfgError(HFG_ERR_NOMEM, "store_integrals: the stored integrals need " + std::to_string(bytes >> 20) +
+                                          " MiB, more than 80% of the free device memory; use the direct build");
+    for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+    {
+        const unsigned long long n = e->h_counts[2 * qc];
+        e->conv_n[qc] = n;
+        if (n == 0)
+            continue;
+        const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+        const int P2 = qc - P1 * (P1 + 1) / 2;
+        const int L  = pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2);
+        const size_t nq = ncart(pair_class_l1(P1)) * ncart(pair_class_l2(P1)) * ncart(pair_class_l1(P2)) * ncart(pair_class_l2(P2));
+        e->d_conv_list[qc].alloc(n);
+        HFG_CUDA(cudaMemcpyAsync(e->d_conv_list[qc].p, e->d_list[qc][0].p, sizeof(Quartet) * n, cudaMemcpyDeviceToDevice,
+                                 e->stream));
+        e->d_conv[qc].alloc(n * nq);
+        ClassLaunch c {};
+        c.list       = e->d_conv_list[qc].p;
+        c.count_dev  = e->d_counts.p + 2 * qc;
+        c.count_host = n;
+        c.view       = base_view(e, false);
+        c.view.pairs = e->d_spairs.p;
+        c.view.store = e->d_conv[qc].p;
+        c.view.ao_thr = 0.0;
+        c.boys_slice = e->d_boys64[L].p;
+        c.tables     = e->d_tables.p;
+        c.stream     = e->stream;
+        c.num_sms    = e->num_sms;
+        c.form       = class_default_form(qc, false);
+        HFG_CUDA(launch_class(qc, c));
+    }
+    HFG_CUDA(cudaStreamSynchronize(e->stream));
+    e->conv_thr = sthr;
+    e->last_valid = false; // the lists of the last direct build were overwritten
+    if (bytes_out)
+        *bytes_out = bytes;
+}
+
+// SCF::buildFockMatrix (src/SCF.cpp:233-521): J[D], K[D] of the FULL densities from the stored integrals,
+// with the AO-level skip |(ij|kl)| < SCHWARTZ_THRESH of the reference's loop.  The request's dD fields
+// carry the full densities here.
+static void fock_conventional(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats* st)
+{
+    if (e->conv_thr < 0.0)
+        throw HfgError(HFG_ERR_INVALID, "fock_conventional: no stored integrals (call hfg_store_integrals first)");
+    if (!r.dD_tot || !r.dD_alpha || !r.J || !r.K_alpha || (r.unrestricted && (!r.dD_beta || !r.K_beta)))
+        throw HfgError(HFG_ERR_INVALID, "fock: missing matrix pointer");
+    const bool uhf     = r.unrestricted != 0;
+    const long long N2 = e->mat_total;
+    const int nspin    = uhf ? 3 : 2;
+    cudaStream_t s     = e->stream;
+    const double* src[3] = {r.dD_tot, r.dD_alpha, r.dD_beta};
+    HFG_CUDA(cudaEventRecord(e->ev[1], s));
+    for (int k = 0; k < nspin; ++k)
+    {
+        HFG_CUDA(cudaMemcpyAsync(e->d_dD[k].p, src[k], sizeof(double) * N2,
+                                 r.device_pointers ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+        HFG_CUDA(cudaMemsetAsync(e->d_acc[k].p, 0, sizeof(double) * N2, s));
+    }
+    int launches = 0;
+    for (int qc = kNumQuartetClasses - 1; qc >= 0; --qc)
+    {
+        if (e->conv_n[qc] == 0)
+            continue;
+        StoredLaunch L {};
+        L.list        = e->d_conv_list[qc].p;
+        L.count       = e->conv_n[qc];
+        L.store       = e->d_conv[qc].p;
+        L.view        = base_view(e, false);
+        L.view.pairs  = e->d_spairs.p;
+        L.view.Dt     = e->d_dD[0].p;
+        L.view.Da     = e->d_dD[1].p;
+        L.view.Db     = e->d_dD[2].p;
+        L.view.X      = e->d_acc[0].p;
+        L.view.Ya     = e->d_acc[1].p;
+        L.view.Yb     = e->d_acc[2].p;
+        L.view.ao_thr = r.schwartz_threshold;
+        L.uhf         = uhf;
+        L.stream      = s;
+        L.num_sms     = e->num_sms;
+        HFG_CUDA(launch_stored(qc, L));
+        ++launches;
+    }
+    double* outs[3] = {r.J, r.K_alpha, r.K_beta};
+    for (int k = 0; k < nspin; ++k)
+    {
+        symmetrize_kernel<<<grid_for(N2, 256, e->num_sms), 256, 0, s>>>(e->d_acc[k].p, e->d_out[k].p, e->d_mat_off.p,
+                                                                          e->d_mat_ld.p, e->nmol, N2);
+        HFG_CUDA(cudaGetLastError());
+        ++launches;
+    }
+    HFG_CUDA(cudaEventRecord(e->ev[6], s));
+    for (int k = 0; k < nspin; ++k)
+        HFG_CUDA(cudaMemcpyAsync(outs[k], e->d_out[k].p, sizeof(double) * N2,
+                                 r.device_pointers ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+    HFG_CUDA(cudaStreamSynchronize(s));
+    if (st)
+    {
+        std::memset(st, 0, sizeof(*st));
+        for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+        {
+            st->quartets_fp64[qc] = e->conv_n[qc];
+            st->form_fp64[qc]     = e->conv_n[qc] ? HFG_FORM_THREAD : 0;
+        }
+        st->kernel_launches = launches;
+        float ms = 0.f;
+        HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[1], e->ev[6]));
+        st->ms_total = ms;
+    }
+}
+
 const hfg_basis* engine_basis(const hfg_engine* e)
 {
     return (e && e->nmol == 1) ? &e->basis[0].view : nullptr;
@@ -1701,6 +1857,68 @@ static double gradient_two_electron(hfg_engine* e, const std::vector<int>& shell
     float ms = 0.f;
     HFG_CUDA(cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]));
     return ms;
+}
+
+// Enqueues one device-pointer Fock build on the engine stream without any host synchronisation, for a
+// caller that captures it into its own CUDA graph (the SCF iteration graph).  The build must have run
+// eagerly once with the same precision, spin case and Schwartz threshold (forms tuned, lists sized,
+// buffers allocated).  The list lengths land in pinned memory; engine_check_counts reads them after the
+// graph has run.  Returns the kernel launches enqueued; throws like the other engine calls.
+int engine_enqueue_fock(hfg_engine* e, const hfg_fock_request& r)
+{
+    if (!r.device_pointers)
+        throw HfgError(HFG_ERR_INVALID, "fock: a captured build needs device pointers");
+    if (!e->have_Q || e->cap_thr != r.schwartz_threshold || (r.precision == HFG_PRECISION_MIXED && !e->cap_mixed) ||
+        !e->h_counts_pin)
+        throw HfgError(HFG_ERR_INVALID, "fock: a captured build needs an eager build with the same request first");
+    int forms[kNumQuartetClasses][2] {};
+    double unused = 0.0;
+    return enqueue_build(e, r, true, forms, &unused);
+}
+
+// Allocates what a captured build writes to on the host (before any capture begins).
+void engine_prepare_capture(hfg_engine* e)
+{
+    if (!e->h_counts_pin)
+        HFG_CUDA(cudaMallocHost(&e->h_counts_pin, sizeof(unsigned long long) * (4 * kNumQuartetClasses + 1)));
+}
+
+// After a graph holding engine_enqueue_fock has run (and the stream is synchronised): the list-overflow
+// check and the survivor counts of that build.
+void engine_check_counts(hfg_engine* e, bool mixed)
+{
+    const int ncnt = kNumQuartetClasses * 2;
+    e->h_counts.assign(e->h_counts_pin, e->h_counts_pin + 2 * ncnt + 1);
+    for (int qc = 0; qc < kNumQuartetClasses; ++qc)
+        if (e->h_counts[2 * qc] > e->cap[qc] || e->h_counts[2 * qc + 1] > e->cap[qc])
+            throw HfgError(HFG_ERR_OVERFLOW, "fock: quartet list overflow");
+    e->last_valid = true;
+    e->last_mixed = mixed ? 1 : 0;
+}
+
+// The engine-call guard for host code outside this file: runs f, maps engine exceptions to HFG codes.
+int engine_guarded(hfg_engine* e, const std::function<void()>& f)
+{
+    try
+    {
+        f();
+        return HFG_OK;
+    }
+    catch (const HfgError& x)
+    {
+        e->last_error = x.what();
+        return x.code;
+    }
+    catch (const std::bad_alloc&)
+    {
+        e->last_error = "host allocation failed";
+        return HFG_ERR_NOMEM;
+    }
+    catch (const std::exception& x)
+    {
+        e->last_error = x.what();
+        return HFG_ERR_INVALID;
+    }
 }
 
 void engine_store_scf_state(hfg_engine* e, const double* Da, const double* Db, const double* W, bool uhf)
@@ -2002,12 +2220,32 @@ int hfg_fock_direct(hfg_engine* e, const hfg_fock_request* req, hfg_fock_stats* 
     });
 }
 
+int hfg_store_integrals(hfg_engine* e, double schwartz_threshold, size_t* bytes)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        hfg::store_integrals(e, schwartz_threshold, bytes);
+    });
+}
+
+int hfg_fock_conventional(hfg_engine* e, const hfg_fock_request* req, hfg_fock_stats* stats)
+{
+    if (!e || !req)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        hfg::fock_conventional(e, *req, stats);
+    });
+}
+
 int hfg_set_kernel_form(hfg_engine* e, int qclass, int fp32, int form)
 {
     if (!e)
         return HFG_ERR_INVALID;
     if (qclass < -1 || qclass >= hfg::kNumQuartetClasses || (fp32 != 0 && fp32 != 1) || form < HFG_FORM_AUTO ||
-        form > HFG_FORM_GROUP)
+        form > HFG_FORM_CHUNK)
     {
         e->last_error = "set_kernel_form: class, precision or form out of range";
         return HFG_ERR_INVALID;
@@ -2045,7 +2283,23 @@ int hfg_set_precision_overlap(hfg_engine* e, int on, double share)
     }
     hfg::invalidate_graph(e);
     e->overlap       = on != 0;
-    e->overlap_share = static_cast<float>(share);
+    e->overlap_share   = static_cast<float>(share);
+    e->overlap_share32 = static_cast<float>(share);
+    return HFG_OK;
+}
+
+int hfg_set_precision_shares(hfg_engine* e, double share_fp64, double share_fp32)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    if (!(share_fp64 > 0.0 && share_fp64 <= 1.0) || !(share_fp32 > 0.0 && share_fp32 <= 1.0))
+    {
+        e->last_error = "set_precision_shares: shares must be in (0, 1]";
+        return HFG_ERR_INVALID;
+    }
+    hfg::invalidate_graph(e);
+    e->overlap_share   = static_cast<float>(share_fp64);
+    e->overlap_share32 = static_cast<float>(share_fp32);
     return HFG_OK;
 }
 

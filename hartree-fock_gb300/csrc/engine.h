@@ -24,11 +24,11 @@ struct ClassLaunch
     bool uhf;
     cudaStream_t stream;
     int num_sms;
-    int form; // 0: the class's default form, else one of kFormThread / kFormWarp / kFormGroup
+    int form; // 0: the class's default form, else one of kFormThread / kFormWarp / kFormGroup / kFormChunk
     float share = 1.f; // fraction of the resident blocks per SM the grid may take (concurrent precisions)
 };
 // Kernel forms of a class kernel (eri_jk.cuh, eri_warp.cuh, eri_group.cuh).
-constexpr int kFormThread = 1, kFormWarp = 2, kFormGroup = 3;
+constexpr int kFormThread = 1, kFormWarp = 2, kFormGroup = 3, kFormChunk = 4;
 using ClassLauncher = cudaError_t (*)(const ClassLaunch&);
 // Defined in classes.cu (one translation unit per quartet class).
 cudaError_t launch_class(int qclass, const ClassLaunch& L);
@@ -36,6 +36,19 @@ cudaError_t launch_class(int qclass, const ClassLaunch& L);
 unsigned class_form_mask(int qclass, bool fp32);
 // The form a launch with form == 0 runs.
 int class_default_form(int qclass, bool fp32);
+
+// Digestion of one class's stored integrals (the stored-integral SCF).
+struct StoredLaunch
+{
+    const Quartet* list;
+    unsigned long long count;
+    const double* store;
+    FockView view;
+    bool uhf;
+    cudaStream_t stream;
+    int num_sms;
+};
+cudaError_t launch_stored(int qclass, const StoredLaunch& L);
 
 struct GradView;
 struct GradLaunch

@@ -136,15 +136,17 @@ template <typename Real, bool SoA> struct RecRef
     }
 };
 
-// Contracted Cartesian integrals of one quartet (without the angular normalisation factors).  KSoA: the
-// ket table tk is field-major with field stride kfs.
-template <int LA, int LB, int LC, int LD, typename Real, bool KSoA = false>
+// Contracted Cartesian integrals of one quartet (without the angular normalisation factors), for the ket
+// components kl in [KL0, KL1) (all of them by default): acc[ij * (KL1 - KL0) + kl - KL0].  KSoA: the ket
+// table tk is field-major with field stride kfs.
+template <int LA, int LB, int LC, int LD, typename Real, bool KSoA = false, int KL0 = 0,
+          int KL1 = ncart(LC) * ncart(LD)>
 __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& ket, const Real* __restrict__ tb,
                                              const Real* __restrict__ tk, const Real* __restrict__ slice,
                                              Real* acc, long long kfs = 0)
 {
     constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD;
-    constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
+    constexpr int NAB = ncart(LA) * ncart(LB), NCD = KL1 - KL0;
     constexpr int HAB = nherm(LAB), HL = nherm(L);
     constexpr int SB = pp_stride(LA, LB), SK = pp_stride(LC, LD);
 #pragma unroll
@@ -185,7 +187,7 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
             Real R[HL];
             hermite_R<L, Real>(Fs, X, Y, Z, R);
 
-            static_for<0, NCD>(
+            static_for<KL0, KL1>(
                 [&](auto KL)
                 {
                     constexpr int kl   = decltype(KL)::value;
@@ -209,7 +211,7 @@ __device__ __forceinline__ void eval_quartet(const PairRec& bra, const PairRec& 
                                     else
                                         s += term;
                                 });
-                            G[h * NCD + kl] += s;
+                            G[h * NCD + (kl - KL0)] += s;
                         });
                 });
         }
@@ -321,17 +323,35 @@ __device__ __forceinline__ void load_digest_d(const PairRec& bra, const PairRec&
     }
 }
 
-// Digestion of one evaluated quartet into X, Ya (, Yb), with its density values already loaded.
+// Ket components kl in [KL0, KL1) that touch ket Cartesian index k (of shell c) or l (of shell d).
+template <int ND, int KL0, int KL1> __host__ __device__ constexpr bool chunk_has_k(int k)
+{
+    for (int kl = KL0; kl < KL1; ++kl)
+        if (kl / ND == k)
+            return true;
+    return false;
+}
+template <int ND, int KL0, int KL1> __host__ __device__ constexpr bool chunk_has_l(int l)
+{
+    for (int kl = KL0; kl < KL1; ++kl)
+        if (kl % ND == l)
+            return true;
+    return false;
+}
+
+// Digestion of one evaluated quartet into X, Ya (, Yb), with its density values already loaded; acc holds
+// the integrals of the ket components kl in [KL0, KL1) (all of them by default), and only the output
+// elements those components reach are added.
 // bra_warp: every lane of the warp calls this together and all active lanes hold the same bra pair;
 // the bra's Coulomb block X_ab is then summed over the warp and added once (inactive lanes pass
 // active = false and acc = 0).  Otherwise each active lane adds its own.
-template <int LA, int LB, int LC, int LD, typename Real, bool UHF>
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF, int KL0 = 0, int KL1 = ncart(LC) * ncart(LD)>
 __device__ __forceinline__ void digest_loaded(const PairRec& bra, const PairRec& ket, bool same_pair, const Real* acc,
                                               const FockView& v, const DigestD<LA, LB, LC, LD, Real, UHF>& d,
                                               bool active, bool bra_warp)
 {
     constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
-    constexpr int NAB = NA * NB, NCD = NC * ND;
+    constexpr int NAB = NA * NB, CH = KL1 - KL0;
     const long long off = v.mat_off[bra.mol];
     const int n         = v.mat_ld[bra.mol];
     const Real s   = (bra.same ? Real(0.5) : Real(1)) * (ket.same ? Real(0.5) : Real(1)) * (same_pair ? Real(0.5) : Real(1));
@@ -339,11 +359,11 @@ __device__ __forceinline__ void digest_loaded(const PairRec& bra, const PairRec&
     const int a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
     auto at = [&](int r, int c) -> long long { return off + r + static_cast<long long>(c) * n; };
 
-    Real Jab[NAB], Jcd[NCD];
+    Real Jab[NAB], Jcd[CH];
 #pragma unroll
     for (int x = 0; x < NAB; ++x) Jab[x] = Real(0);
 #pragma unroll
-    for (int x = 0; x < NCD; ++x) Jcd[x] = Real(0);
+    for (int x = 0; x < CH; ++x) Jcd[x] = Real(0);
 
     constexpr int nspin = UHF ? 2 : 1;
 #pragma unroll
@@ -367,50 +387,68 @@ __device__ __forceinline__ void digest_loaded(const PairRec& bra, const PairRec&
                     [&](auto Jx)
                     {
                         constexpr int j = decltype(Jx)::value;
-                        static_for<0, NC>(
-                            [&](auto Kx)
+                        static_for<KL0, KL1>(
+                            [&](auto KLx)
                             {
-                                constexpr int k = decltype(Kx)::value;
-                                static_for<0, ND>(
-                                    [&](auto Lx)
-                                    {
-                                        constexpr int l = decltype(Lx)::value;
-                                        constexpr Real an = Real(ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k)
-                                                                 * ang_norm(LD, l));
-                                        const Real eri = acc[(i * NB + j) * NCD + k * ND + l] * an;
-                                        const Real w   = (fabs(eri) < thr) ? Real(0) : s * eri;
-                                        if (spin == 0)
-                                        {
-                                            Jab[i * NB + j] += w * d.Dcd[k * ND + l];
-                                            Jcd[k * ND + l] += w * d.Dab[i * NB + j];
-                                        }
-                                        Kac[i * NC + k] += w * d.Dbd[spin][j * ND + l];
-                                        Kad[i * ND + l] += w * d.Dbc[spin][j * NC + k];
-                                        Kbc[j * NC + k] += w * d.Dad[spin][i * ND + l];
-                                        Kbd[j * ND + l] += w * d.Dac[spin][i * NC + k];
-                                    });
+                                constexpr int kl = decltype(KLx)::value;
+                                constexpr int k = kl / ND, l = kl % ND;
+                                constexpr Real an = Real(ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k)
+                                                         * ang_norm(LD, l));
+                                const Real eri = acc[(i * NB + j) * CH + (kl - KL0)] * an;
+                                const Real w   = (fabs(eri) < thr) ? Real(0) : s * eri;
+                                if (spin == 0)
+                                {
+                                    Jab[i * NB + j] += w * d.Dcd[k * ND + l];
+                                    Jcd[kl - KL0] += w * d.Dab[i * NB + j];
+                                }
+                                Kac[i * NC + k] += w * d.Dbd[spin][j * ND + l];
+                                Kad[i * ND + l] += w * d.Dbc[spin][j * NC + k];
+                                Kbc[j * NC + k] += w * d.Dad[spin][i * ND + l];
+                                Kbd[j * ND + l] += w * d.Dac[spin][i * NC + k];
                             });
                     });
             });
         if (active)
         {
             double* Y = spin == 0 ? v.Ya : v.Yb;
-#pragma unroll
-            for (int i = 0; i < NA; ++i)
-            {
-#pragma unroll
-                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(a0 + i, c0 + k), widen(Kac[i * NC + k]));
-#pragma unroll
-                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(a0 + i, d0 + l), widen(Kad[i * ND + l]));
-            }
-#pragma unroll
-            for (int j = 0; j < NB; ++j)
-            {
-#pragma unroll
-                for (int k = 0; k < NC; ++k) atomicAdd(Y + at(b0 + j, c0 + k), widen(Kbc[j * NC + k]));
-#pragma unroll
-                for (int l = 0; l < ND; ++l) atomicAdd(Y + at(b0 + j, d0 + l), widen(Kbd[j * ND + l]));
-            }
+            static_for<0, NA>(
+                [&](auto I)
+                {
+                    constexpr int i = decltype(I)::value;
+                    static_for<0, NC>(
+                        [&](auto Kx)
+                        {
+                            constexpr int k = decltype(Kx)::value;
+                            if constexpr (chunk_has_k<ND, KL0, KL1>(k))
+                                atomicAdd(Y + at(a0 + i, c0 + k), widen(Kac[i * NC + k]));
+                        });
+                    static_for<0, ND>(
+                        [&](auto Lx)
+                        {
+                            constexpr int l = decltype(Lx)::value;
+                            if constexpr (chunk_has_l<ND, KL0, KL1>(l))
+                                atomicAdd(Y + at(a0 + i, d0 + l), widen(Kad[i * ND + l]));
+                        });
+                });
+            static_for<0, NB>(
+                [&](auto Jx)
+                {
+                    constexpr int j = decltype(Jx)::value;
+                    static_for<0, NC>(
+                        [&](auto Kx)
+                        {
+                            constexpr int k = decltype(Kx)::value;
+                            if constexpr (chunk_has_k<ND, KL0, KL1>(k))
+                                atomicAdd(Y + at(b0 + j, c0 + k), widen(Kbc[j * NC + k]));
+                        });
+                    static_for<0, ND>(
+                        [&](auto Lx)
+                        {
+                            constexpr int l = decltype(Lx)::value;
+                            if constexpr (chunk_has_l<ND, KL0, KL1>(l))
+                                atomicAdd(Y + at(b0 + j, d0 + l), widen(Kbd[j * ND + l]));
+                        });
+                });
         }
     }
     if (bra_warp)
@@ -437,9 +475,8 @@ __device__ __forceinline__ void digest_loaded(const PairRec& bra, const PairRec&
     if (active)
     {
 #pragma unroll
-        for (int k = 0; k < NC; ++k)
-#pragma unroll
-            for (int l = 0; l < ND; ++l) atomicAdd(v.X + at(c0 + k, d0 + l), widen(Real(2) * Jcd[k * ND + l]));
+        for (int x = 0; x < CH; ++x)
+            atomicAdd(v.X + at(c0 + (KL0 + x) / ND, d0 + (KL0 + x) % ND), widen(Real(2) * Jcd[x]));
     }
 }
 
@@ -521,6 +558,168 @@ __global__ void __launch_bounds__(128) jk_class_kernel(const Quartet* __restrict
         const bool bra_warp = __all_sync(0xffffffffu, qt.bra == bra0);
         digest_loaded<LA, LB, LC, LD, Real, UHF>(bra, ket, qt.bra == qt.ket, acc, v, d, active, bra_warp);
     }
+}
+
+// Ket-chunked thread form: one thread per (shell quartet, chunk of CH ket Cartesian components).  For the
+// d-containing classes a thread cannot hold a whole quartet's G[HAB][NCD] and ERI[NAB][NCD] in registers;
+// restricted to CH ket components the thread keeps R, G[HAB][CH] and ERI[NAB][CH] in registers, with every
+// loop unrolled at compile time, and digests the integrals of its chunk (the bra Coulomb block summed over
+// the warp as in the thread form; the exchange and ket Coulomb elements its chunk reaches).  The chunks
+// of a quartet run in neighbouring blocks (block b: chunk b % NCH), so they share the quartet's records in
+// L1/L2.  Each chunk recomputes the Boys values and R of its quartet: for FP32, where these are cheap
+// next to the two Hermite transforms, that buys full lanes and no shared-memory round trips.
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF, int KL0, int KL1>
+__device__ __forceinline__ void chunk_body(const Quartet* __restrict__ list, unsigned long long n, const FockView& v,
+                                           const Real* __restrict__ slice, unsigned qb, unsigned nqb)
+{
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    constexpr int NAB = NA * NB, NCD = NC * ND, CH = KL1 - KL0;
+    const Real* tb      = static_cast<const Real*>(v.pptab[pair_class(LA, LB)]);
+    const Real* tk      = static_cast<const Real*>(v.ksoa[pair_class(LC, LD)]);
+    const long long kfs = v.kfs[pair_class(LC, LD)];
+    using DD       = DigestD<LA, LB, LC, LD, Real, UHF>;
+    const int lane = threadIdx.x & 31;
+    for (unsigned long long base = static_cast<unsigned long long>(qb) * blockDim.x + (threadIdx.x & ~31u); base < n;
+         base += static_cast<unsigned long long>(nqb) * blockDim.x)
+    {
+        const unsigned long long q = base + lane;
+        const bool active          = q < n;
+        const Quartet qt           = list[active ? q : base];
+        const PairRec bra          = v.pairs[qt.bra];
+        const PairRec ket          = v.pairs[qt.ket];
+        Real acc[NAB * CH];
+        if (active)
+            eval_quartet<LA, LB, LC, LD, Real, true, KL0, KL1>(bra, ket, tb, tk, slice, acc, kfs);
+        else
+        {
+#pragma unroll
+            for (int x = 0; x < NAB * CH; ++x) acc[x] = Real(0);
+        }
+        if (v.store != nullptr)
+        {
+            if (active)
+                static_for<0, NAB>(
+                    [&](auto IJ)
+                    {
+                        constexpr int ij = decltype(IJ)::value;
+                        static_for<KL0, KL1>(
+                            [&](auto KLx)
+                            {
+                                constexpr int kl = decltype(KLx)::value;
+                                constexpr double an = ang_norm(LA, ij / NB) * ang_norm(LB, ij % NB) *
+                                                      ang_norm(LC, kl / ND) * ang_norm(LD, kl % ND);
+                                v.store[q * (NAB * NCD) + ij * NCD + kl] = double(acc[ij * CH + (kl - KL0)]) * an;
+                            });
+                    });
+            continue;
+        }
+        DD d;
+        load_digest_d<LA, LB, LC, LD, Real, UHF>(bra, ket, v, d); // values the chunk does not read are never loaded
+        const unsigned bra0 = __shfl_sync(0xffffffffu, qt.bra, 0);
+        const bool bra_warp = __all_sync(0xffffffffu, qt.bra == bra0);
+        digest_loaded<LA, LB, LC, LD, Real, UHF, KL0, KL1>(bra, ket, qt.bra == qt.ket, acc, v, d, active, bra_warp);
+    }
+}
+
+// Blocks of the chunked form: NCH consecutive blocks hold the NCH chunks of the same 128 quartets.
+template <int LC, int LD, int CH> __host__ __device__ constexpr int num_chunks()
+{
+    return (ncart(LC) * ncart(LD) + CH - 1) / CH;
+}
+
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF, int CH>
+__global__ void __launch_bounds__(128) jk_class_chunk_kernel(const Quartet* __restrict__ list,
+                                                             const unsigned long long* __restrict__ count, FockView v,
+                                                             const Real* __restrict__ boys_slice)
+{
+    constexpr int NCD = ncart(LC) * ncart(LD), NCH = num_chunks<LC, LD, CH>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real* slice                = reinterpret_cast<Real*>(smem_raw);
+    const unsigned long long n = *count;
+    const unsigned qb = blockIdx.x / NCH, nqb = gridDim.x / NCH;
+    const int chunk   = static_cast<int>(blockIdx.x % NCH);
+    if (qb >= nqb || static_cast<unsigned long long>(qb) * blockDim.x >= n)
+        return;
+    stage_boys<Real>(boys_slice, slice);
+    static_for<0, NCH>(
+        [&](auto C)
+        {
+            constexpr int c = decltype(C)::value;
+            if (chunk == c)
+                chunk_body<LA, LB, LC, LD, Real, UHF, c * CH, (c * CH + CH < NCD ? c * CH + CH : NCD)>(list, n, v, slice,
+                                                                                                      qb, nqb);
+        });
+}
+
+// Digestion of stored integrals (the stored-integral SCF): integral blocks written once in store mode
+// (row-major [ij][kl] per quartet, angular factors included) are digested with full densities every
+// build.  Ket-chunked like jk_class_chunk_kernel so that the integrals and partial sums of a thread stay
+// in registers: a thread digests ket components [KL0, KL1) of one quartet.
+template <int LA, int LB, int LC, int LD, bool UHF, int KL0, int KL1>
+__device__ __forceinline__ void stored_body(const Quartet* __restrict__ list, unsigned long long n, const FockView& v,
+                                            const double* __restrict__ store, unsigned qb, unsigned nqb)
+{
+    constexpr int NA = ncart(LA), NB = ncart(LB), NC = ncart(LC), ND = ncart(LD);
+    constexpr int NAB = NA * NB, NCD = NC * ND, CH = KL1 - KL0;
+    using DD       = DigestD<LA, LB, LC, LD, double, UHF>;
+    const int lane = threadIdx.x & 31;
+    for (unsigned long long base = static_cast<unsigned long long>(qb) * blockDim.x + (threadIdx.x & ~31u); base < n;
+         base += static_cast<unsigned long long>(nqb) * blockDim.x)
+    {
+        const unsigned long long q = base + lane;
+        const bool active          = q < n;
+        const Quartet qt           = list[active ? q : base];
+        const PairRec bra          = v.pairs[qt.bra];
+        const PairRec ket          = v.pairs[qt.ket];
+        double acc[NAB * CH];
+        const double* __restrict__ blk = store + (active ? q : base) * static_cast<unsigned long long>(NAB * NCD);
+        static_for<0, NAB>(
+            [&](auto IJ)
+            {
+                constexpr int ij = decltype(IJ)::value;
+                static_for<KL0, KL1>(
+                    [&](auto KLx)
+                    {
+                        constexpr int kl = decltype(KLx)::value;
+                        // The digestion multiplies by the angular factors again.
+                        constexpr double inv_an = 1.0 / (ang_norm(LA, ij / NB) * ang_norm(LB, ij % NB) *
+                                                         ang_norm(LC, kl / ND) * ang_norm(LD, kl % ND));
+                        acc[ij * CH + (kl - KL0)] = active ? blk[ij * NCD + kl] * inv_an : 0.0;
+                    });
+            });
+        DD d;
+        load_digest_d<LA, LB, LC, LD, double, UHF>(bra, ket, v, d);
+        const unsigned bra0 = __shfl_sync(0xffffffffu, qt.bra, 0);
+        const bool bra_warp = __all_sync(0xffffffffu, qt.bra == bra0);
+        digest_loaded<LA, LB, LC, LD, double, UHF, KL0, KL1>(bra, ket, qt.bra == qt.ket, acc, v, d, active, bra_warp);
+    }
+}
+
+// Ket components per thread of the stored digestion: at most 36 integrals per thread.
+template <int LA, int LB, int LC, int LD> __host__ __device__ constexpr int stored_chunk()
+{
+    constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
+    constexpr int c   = 36 / NAB > 0 ? 36 / NAB : 1;
+    return c < NCD ? c : NCD;
+}
+
+template <int LA, int LB, int LC, int LD, bool UHF>
+__global__ void __launch_bounds__(128) jk_stored_kernel(const Quartet* __restrict__ list, unsigned long long n,
+                                                        FockView v, const double* __restrict__ store)
+{
+    constexpr int NCD = ncart(LC) * ncart(LD), CH = stored_chunk<LA, LB, LC, LD>(), NCH = num_chunks<LC, LD, CH>();
+    const unsigned qb = blockIdx.x / NCH, nqb = gridDim.x / NCH;
+    const int chunk   = static_cast<int>(blockIdx.x % NCH);
+    if (qb >= nqb || static_cast<unsigned long long>(qb) * blockDim.x >= n)
+        return;
+    static_for<0, NCH>(
+        [&](auto C)
+        {
+            constexpr int c = decltype(C)::value;
+            if (chunk == c)
+                stored_body<LA, LB, LC, LD, UHF, c * CH, (c * CH + CH < NCD ? c * CH + CH : NCD)>(list, n, v, store, qb,
+                                                                                                nqb);
+        });
 }
 
 } // namespace hfg

@@ -11,6 +11,7 @@
 // Only the two-electron build is replaced (hfg_fock_direct on device pointers).  The orbital
 // eigenvectors come from cuSOLVER's syevd (ascending eigenvalues, as Eigen's SelfAdjointEigenSolver).
 #include "hfgpu.h"
+#include "scf_device.h"
 
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
@@ -21,6 +22,7 @@
 #include <cmath>
 #include <cstdio>
 #include <deque>
+#include <functional>
 #include <limits>
 #include <stdexcept>
 #include <string>
@@ -34,6 +36,10 @@ namespace hfg
 const hfg_basis* engine_basis(const hfg_engine* e);
 void engine_set_error(hfg_engine* e, const std::string& msg);
 void engine_store_scf_state(hfg_engine* e, const double* Da, const double* Db, const double* W, bool uhf);
+int engine_enqueue_fock(hfg_engine* e, const hfg_fock_request& r);
+void engine_prepare_capture(hfg_engine* e);
+void engine_check_counts(hfg_engine* e, bool mixed);
+int engine_guarded(hfg_engine* e, const std::function<void()>& f);
 
 namespace
 {
@@ -137,6 +143,7 @@ class Scf
 
     ~Scf()
     {
+        free_device_iterations();
         if (info_)
             cudaFree(info_);
         if (cs_)
@@ -198,21 +205,40 @@ class Scf
             std::printf("%15s%15s%15s%15s\n", "Iteration", "dE", "dD", "DIIS Error");
         int it = 0;
         bool conv = false;
+        // Device iterations (DIIS and the measures on the GPU) when the options allow a graph; the first
+        // runs eagerly (it tunes the kernel forms and sizes the lists), the next is captured, and every
+        // later one replays that graph.
+        if (o_.direct == 0)
+        {
+            // SCF::initialize (SCF.cpp:157-159): the integrals are computed once before the iterations.
+            const int rc = hfg_store_integrals(eng_, o_.schwartz_threshold, nullptr);
+            if (rc != HFG_OK)
+                throw ScfError(rc, std::string("scf: storing the integrals failed: ") + hfg_last_error(eng_));
+        }
+        const bool device_iter = o_.direct != 0 && o_.graph_iterations != 0 && o_.damp == 0 && !(o_.level_shift > 0) &&
+                                 (!o_.use_diis || o_.diis_size <= kDiisMaxSize) && o_.full_rebuild_every == 0;
+        if (device_iter)
+            setup_device_iterations();
         for (it = 0; it < o_.max_iter; ++it)
         {
-            const double lastE = energy_;
-            fock(it);
-            if (o_.use_diis)
+            if (device_iter)
+                device_iteration(it);
+            else
             {
-                diis_update();
-                diis_extrapolate();
+                const double lastE = energy_;
+                fock(it);
+                if (o_.use_diis)
+                {
+                    diis_update();
+                    diis_extrapolate();
+                }
+                diagonalize_update(it);
+                dE_ = std::fabs(energy_ - lastE);
+                add(T1_, 1.0, Dt_, -1.0, Dtp_);
+                dD_ = nrm(T1_);
+                if (o_.use_diis)
+                    diis_err_ = hist_.empty() ? 0.0 : nrm(hist_.back().e);
             }
-            diagonalize_update(it);
-            dE_ = std::fabs(energy_ - lastE);
-            add(T1_, 1.0, Dt_, -1.0, Dtp_);
-            dD_ = nrm(T1_);
-            if (o_.use_diis)
-                diis_err_ = hist_.empty() ? 0.0 : nrm(hist_.back().e);
             if (o_.verbose)
                 std::printf("%15d%15.5e%15.5e%15.5e\n", it + 1, dE_, dD_, diis_err_);
             if (dE_ < o_.energy_tol && dD_ < o_.density_tol && (!o_.use_diis || diis_err_ < o_.diis_tol))
@@ -222,6 +248,15 @@ class Scf
             }
         }
         ck(cudaStreamSynchronize(s_), "sync");
+        if (device_iter)
+        {
+            int info = 0;
+            ck(cudaMemcpy(&info, info_, sizeof(int), cudaMemcpyDeviceToHost), "d2h");
+            if (info != 0)
+                throw ScfError(HFG_ERR_CUDA, "scf: syevd did not converge (info " + std::to_string(info) + ")");
+            eig_host();
+        }
+        res.graph_replays = replays_;
         const auto t1 = std::chrono::steady_clock::now();
         res.e_electronic = energy_;
         res.e_nuclear    = enuc_;
@@ -410,10 +445,12 @@ class Scf
         ck(cudaMemcpyAsync(wb_h_.data(), wb_.p, sizeof(double) * n_, cudaMemcpyDeviceToHost, s_), "d2h");
         ck(cudaStreamSynchronize(s_), "sync");
     }
-    // SCF::buildFockMatrixDirect with the GPU build; F = F_prev + J - K (SCF.cpp:731-743).
+    // SCF::buildFockMatrixDirect with the GPU build; F = F_prev + J - K (SCF.cpp:731-743).  DIRECT FALSE:
+    // SCF::buildFockMatrix from the stored integrals, F = h + J[D] - K[D] (SCF.cpp:233-521).
     void fock(int it)
     {
-        const bool full = o_.full_rebuild_every > 0 && it > 0 && it % o_.full_rebuild_every == 0;
+        const bool conv = o_.direct == 0;
+        const bool full = conv || (o_.full_rebuild_every > 0 && it > 0 && it % o_.full_rebuild_every == 0);
         if (full)
         {
             copy(dDt_, Dt_);
@@ -441,7 +478,7 @@ class Scf
         r.K_alpha            = Ka_.p;
         r.K_beta             = uhf_ ? Kb_.p : nullptr;
         hfg_fock_stats st {};
-        const int rc = hfg_fock_direct(eng_, &r, &st);
+        const int rc = conv ? hfg_fock_conventional(eng_, &r, &st) : hfg_fock_direct(eng_, &r, &st);
         if (rc != HFG_OK)
             throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
         ms_fock_ += st.ms_total;
@@ -599,6 +636,271 @@ class Scf
         energy_ = electronic_energy();
         eig_host();
     }
+    // ---- Device iterations (graph_iterations): DIIS, energy and convergence measures on the GPU ----------
+    DMat ring_[3 * kDiisMaxSize];        // DIIS slots: F_alpha, F_beta, e
+    DMat Bm_, part_, wsc_a_, wsc_b_, dd_; // B per slot pair, partial sums, energy operands, density change
+    DiisState* dstate_   = nullptr;
+    ScfScalars* dsc_     = nullptr;
+    ScfScalars* hsc_     = nullptr; // pinned
+    const double** dptr_ = nullptr; // device pointer tables: [cap] x_e, [cap] y_slots, [3] xs, [3] ys
+    void* cublas_ws_     = nullptr;
+    DiisDevice dd_dev_ {};
+    MeasureDevice md_ {};
+    cudaGraph_t graph_         = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    bool graph_failed_          = false;
+    int replays_                = 0;
+    cudaEvent_t gev_[2] {};
+
+    void setup_device_iterations()
+    {
+        const size_t N2 = static_cast<size_t>(n_) * n_;
+        const int cap   = o_.use_diis ? o_.diis_size : 1;
+        int sms = 0, dev = 0;
+        ck(cudaGetDevice(&dev), "device");
+        ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+        const int nblk = dot_blocks(sms);
+        for (int k = 0; k < 3 * cap; ++k)
+        {
+            ring_[k].alloc(N2);
+            ck(cudaMemsetAsync(ring_[k].p, 0, sizeof(double) * N2, s_), "memset");
+        }
+        Bm_.alloc(static_cast<size_t>(cap) * cap);
+        ck(cudaMemsetAsync(Bm_.p, 0, sizeof(double) * cap * cap, s_), "memset");
+        part_.alloc(static_cast<size_t>(std::max(cap, 3)) * nblk);
+        wsc_a_.alloc(N2);
+        wsc_b_.alloc(N2);
+        dd_.alloc(N2);
+        ck(cudaMalloc(&dstate_, sizeof(DiisState)), "cudaMalloc");
+        ck(cudaMalloc(&dsc_, sizeof(ScfScalars)), "cudaMalloc");
+        ck(cudaMallocHost(&hsc_, sizeof(ScfScalars)), "cudaMallocHost");
+        ck(cudaMalloc(&dptr_, sizeof(double*) * (2 * cap + 6)), "cudaMalloc");
+        DiisState st {};
+        st.cap = cap;
+        ck(cudaMemcpyAsync(dstate_, &st, sizeof(st), cudaMemcpyHostToDevice, s_), "h2d");
+        std::vector<const double*> tab(2 * cap + 6);
+        for (int k = 0; k < cap; ++k)
+        {
+            tab[k]       = e_.p; // the new error vector, built in e_ every iteration
+            tab[cap + k] = ring_[2 * cap + k].p;
+        }
+        tab[2 * cap + 0] = Da_.p;
+        tab[2 * cap + 1] = Db_.p;
+        tab[2 * cap + 2] = dd_.p;
+        tab[2 * cap + 3] = wsc_a_.p;
+        tab[2 * cap + 4] = wsc_b_.p;
+        tab[2 * cap + 5] = dd_.p;
+        ck(cudaMemcpyAsync(dptr_, tab.data(), sizeof(double*) * tab.size(), cudaMemcpyHostToDevice, s_), "h2d");
+        dd_dev_.state = dstate_;
+        for (int k = 0; k < cap; ++k)
+        {
+            dd_dev_.slots.Fa[k] = ring_[k].p;
+            dd_dev_.slots.Fb[k] = ring_[cap + k].p;
+            dd_dev_.slots.e[k]  = ring_[2 * cap + k].p;
+        }
+        dd_dev_.B        = Bm_.p;
+        dd_dev_.xs_e     = dptr_;
+        dd_dev_.ys_slots = dptr_ + cap;
+        dd_dev_.part     = part_.p;
+        dd_dev_.cap      = cap;
+        dd_dev_.nblk     = nblk;
+        dd_dev_.num_sms  = sms;
+        md_ = MeasureDevice {h_.p, Fa_.p, Fb_.p, Dt_.p, Dtp_.p, wsc_a_.p, wsc_b_.p, dd_.p, dptr_ + 2 * cap,
+                             dptr_ + 2 * cap + 3, part_.p, dsc_, nblk, sms};
+        // cuBLAS gets its own workspace, so that no call inside a capture allocates.
+        const size_t ws = 32u << 20;
+        ck(cudaMalloc(&cublas_ws_, ws), "cudaMalloc");
+        ck(cublasSetWorkspace(cb_, cublas_ws_, ws), "cublasSetWorkspace");
+        for (auto& ev : gev_) ck(cudaEventCreate(&ev), "event");
+        engine_prepare_capture(eng_);
+        // The guess's energy is the first "previous" energy of the measures.
+        ck(scf_measures(md_, static_cast<long long>(N2), s_), "measures");
+    }
+
+    void free_device_iterations()
+    {
+        if (graph_exec_)
+            cudaGraphExecDestroy(graph_exec_);
+        if (graph_)
+            cudaGraphDestroy(graph_);
+        for (auto& ev : gev_)
+            if (ev)
+                cudaEventDestroy(ev);
+        if (dstate_)
+            cudaFree(dstate_);
+        if (dsc_)
+            cudaFree(dsc_);
+        if (hsc_)
+            cudaFreeHost(hsc_);
+        if (dptr_)
+            cudaFree(dptr_);
+        if (cublas_ws_)
+            cudaFree(cublas_ws_);
+    }
+
+    // One iteration's work on the stream, no host synchronisation when `capture`: dD, the Fock build,
+    // F = F_prev + J - K, DIIS (device), the orbital step without damping or level shift, the measures and
+    // their copy to pinned memory.
+    void enqueue_iteration(bool capture)
+    {
+        const long long N2 = static_cast<long long>(n_) * n_;
+        add(dDt_, 1.0, Dt_, -1.0, Dtp_);
+        add(dDa_, 1.0, Da_, -1.0, Dap_);
+        if (uhf_)
+            add(dDb_, 1.0, Db_, -1.0, Dbp_);
+        hfg_fock_request r {};
+        r.unrestricted       = uhf_ ? 1 : 0;
+        r.precision          = o_.precision;
+        r.device_pointers    = 1;
+        r.schwartz_threshold = o_.schwartz_threshold;
+        r.density_threshold  = o_.density_threshold;
+        r.fp32_cutoff        = o_.fp32_cutoff;
+        r.dD_tot             = dDt_.p;
+        r.dD_alpha           = dDa_.p;
+        r.dD_beta            = uhf_ ? dDb_.p : nullptr;
+        r.J                  = J_.p;
+        r.K_alpha            = Ka_.p;
+        r.K_beta             = uhf_ ? Kb_.p : nullptr;
+        if (capture)
+        {
+            ck(cudaEventRecord(gev_[0], s_), "event");
+            const int rc = engine_guarded(eng_, [&] { engine_enqueue_fock(eng_, r); });
+            if (rc != HFG_OK)
+                throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
+            ck(cudaEventRecord(gev_[1], s_), "event");
+        }
+        else
+        {
+            hfg_fock_stats st {};
+            const int rc = hfg_fock_direct(eng_, &r, &st);
+            if (rc != HFG_OK)
+                throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
+            ms_fock_ += st.ms_total;
+        }
+        add(Fa_, 1.0, Fap_, 1.0, J_);
+        add(Fa_, 1.0, Fa_, -1.0, Ka_);
+        copy(Fap_, Fa_);
+        if (uhf_)
+        {
+            add(Fb_, 1.0, Fbp_, 1.0, J_);
+            add(Fb_, 1.0, Fb_, -1.0, Kb_);
+            copy(Fbp_, Fb_);
+        }
+        else
+        {
+            copy(Fb_, Fa_);
+            copy(Fbp_, Fap_);
+        }
+        if (o_.use_diis)
+        {
+            // e = (F_a D_a S - S D_a F_a) + (beta) into e_, as diis_update does.
+            const double one = 1.0, mone = -1.0;
+            auto comm = [&](const DMat& F, const DMat& D, bool accumulate) {
+                gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, F.p, D.p, 0.0, T1_.p);
+                gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, T1_.p, S_.p, 0.0, T2_.p);
+                ck(cublasDgeam(cb_, CUBLAS_OP_N, CUBLAS_OP_T, n_, n_, &one, T2_.p, n_, &mone, T2_.p, n_, T1_.p, n_), "geam");
+                if (accumulate)
+                    add(e_, 1.0, e_, 1.0, T1_);
+                else
+                    copy(e_, T1_);
+            };
+            comm(Fa_, Da_, false);
+            comm(Fb_, Db_, true);
+            ck(hfg::diis_push(dd_dev_, Fa_.p, Fb_.p, e_.p, N2, s_), "diis_push");
+            ck(hfg::diis_extrapolate(dd_dev_, Fa_.p, Fb_.p, dsc_, N2, s_), "diis_extrapolate");
+        }
+        // Orbital step (SCF.cpp:747-835 without damping and level shifting).
+        eig_orth_nosync(Fa_, Ca_, wa_);
+        copy(Dap_, Da_);
+        density(Ca_, nocc_a_, Da_, 0.0);
+        copy(Dbp_, Db_);
+        if (uhf_)
+        {
+            eig_orth_nosync(Fb_, Cb_, wb_);
+            density(Cb_, nocc_b_, Db_, 0.0);
+        }
+        else
+        {
+            copy(Cb_, Ca_);
+            copy_vec(wb_, wa_);
+            copy(Db_, Da_);
+        }
+        copy(Dtp_, Dt_);
+        add(Dt_, 1.0, Da_, 1.0, Db_);
+        ck(scf_measures(md_, N2, s_), "measures");
+        ck(cudaMemcpyAsync(hsc_, dsc_, sizeof(ScfScalars), cudaMemcpyDeviceToHost, s_), "d2h");
+    }
+
+    void read_measures()
+    {
+        ck(cudaStreamSynchronize(s_), "sync");
+        energy_ = hsc_->energy;
+        dE_     = hsc_->delta_e;
+        dD_     = hsc_->delta_d;
+        if (o_.use_diis)
+            diis_err_ = hsc_->diis_error;
+    }
+
+    void device_iteration(int it)
+    {
+        ++builds_;
+        if (it > 0 && !graph_exec_ && !graph_failed_)
+        {
+            // Capture this iteration; if the capture is refused (a call inside cannot be captured), run the
+            // rest eagerly.  Nothing of a refused capture has run, so the iteration is then done eagerly.
+            ck(cudaStreamBeginCapture(s_, cudaStreamCaptureModeRelaxed), "begin capture");
+            bool ok = true;
+            try
+            {
+                enqueue_iteration(true);
+            }
+            catch (const ScfError&)
+            {
+                ok = false;
+            }
+            cudaGraph_t g      = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(s_, &g);
+            if (ok && e == cudaSuccess && g && cudaGraphInstantiate(&graph_exec_, g, 0) == cudaSuccess)
+                graph_ = g;
+            else
+            {
+                if (g)
+                    cudaGraphDestroy(g);
+                graph_exec_   = nullptr;
+                graph_failed_ = true;
+                cudaGetLastError(); // clear the refused capture's error state
+            }
+        }
+        if (graph_exec_)
+        {
+            ck(cudaGraphLaunch(graph_exec_, s_), "graph launch");
+            read_measures();
+            const int rc = engine_guarded(eng_, [&] { engine_check_counts(eng_, o_.precision == HFG_PRECISION_MIXED); });
+            if (rc != HFG_OK)
+                throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, gev_[0], gev_[1]) == cudaSuccess)
+                ms_fock_ += ms;
+            ++replays_;
+        }
+        else
+        {
+            enqueue_iteration(false);
+            read_measures();
+        }
+    }
+
+    // eig_orth without level shift and without the host read of syevd's status (checked after the loop).
+    void eig_orth_nosync(const DMat& F, DMat& C, DMat& w)
+    {
+        gemm(CUBLAS_OP_T, CUBLAS_OP_N, n_, n_, n_, 1.0, X_.p, F.p, 0.0, T2_.p);
+        gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, T2_.p, X_.p, 0.0, T1_.p);
+        ck(cusolverDnDsyevd(cs_, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n_, T1_.p, n_, w.p, work_.p, lwork_,
+                            info_),
+           "syevd");
+        gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, X_.p, T1_.p, 0.0, C.p);
+    }
+
     // <S^2> = Sz(Sz+1) + N_beta - |C_a,occ^T S C_b,occ|^2 (SCF.cpp:838-845).
     double spin_squared()
     {
@@ -671,6 +973,8 @@ void hfg_scf_default_options(hfg_scf_options* o, int multiplicity)
     o->fp32_cutoff        = 1e-4; // tuned: (H2O)_64 RHF/6-31G** SCF |dE| = 4.4e-8 Eh vs FP64
     o->full_rebuild_every = 0;
     o->verbose            = 0;
+    o->graph_iterations   = 0;
+    o->direct             = 1;
 }
 
 int hfg_scf_run(hfg_engine* e, const hfg_scf_options* opt, int natom, const int* Z, const double* xyz, int charge,

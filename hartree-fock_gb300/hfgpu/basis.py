@@ -10,6 +10,12 @@ Follows the reference's rules exactly (src/Basis.cpp):
 * Cartesian components with the x exponent descending, then y descending (Basis.cpp:48-59);
 * per primitive and component the factor (2a/pi)^{3/4} (4a)^{l/2} / sqrt((2i-1)!!(2j-1)!!(2k-1)!!)
   (Basis.cpp:61-77); contraction coefficients are not renormalised.
+
+Opt-in extension (``general_contractions=True``; changes the numbers against the reference): a generally
+contracted shell -- one angular momentum with several coefficient rows, e.g. the s and p shells of the
+cc-pVXZ sets -- becomes one shell per coefficient row, each holding the exponents whose coefficient in
+that row is non-zero.  Shells that list several angular momenta (the Pople sp shells) keep the reference
+rule of one row per angular momentum.
 """
 from __future__ import annotations
 
@@ -38,7 +44,7 @@ def cart_components(l: int):
     return [(i, j, l - i - j) for i in range(l, -1, -1) for j in range(l - i, -1, -1)]
 
 
-def read_shells(name: str, elements, directory: str | None = None):
+def read_shells(name: str, elements, directory: str | None = None, general_contractions: bool = False):
     """{Z: [(l, exponents, coefficients), ...]} for the requested elements."""
     path = basis_file(name, directory)
     if not os.path.exists(path):
@@ -53,16 +59,23 @@ def read_shells(name: str, elements, directory: str | None = None):
         shells = []
         for sh in el["electron_shells"]:
             exps = [float(x) for x in sh["exponents"]]
-            for i, l in enumerate(sh["angular_momentum"]):
+            ams = sh["angular_momentum"]
+            if general_contractions and len(ams) == 1 and len(sh["coefficients"]) > 1:
+                for row in sh["coefficients"]:
+                    keep = [(a, float(c)) for a, c in zip(exps, row) if float(c) != 0.0]
+                    shells.append((int(ams[0]), [a for a, _ in keep], [c for _, c in keep]))
+                continue
+            for i, l in enumerate(ams):
                 coefs = [float(x) for x in sh["coefficients"][i]]
                 shells.append((int(l), exps, coefs))
         out[Z] = shells
     return out
 
 
-def pack(name: str, Z, xyz, directory: str | None = None) -> dict:
-    """The engine's SoA for a molecule (atoms Z at xyz, bohr)."""
-    table = read_shells(name, Z, directory)
+def pack(name: str, Z, xyz, directory: str | None = None, general_contractions: bool = False) -> dict:
+    """The engine's SoA for a molecule (atoms Z at xyz, bohr); see the module notes for the opt-in
+    ``general_contractions``."""
+    table = read_shells(name, Z, directory, general_contractions)
     l_, nprim, prim_off, ao_off, norm_off, centers = [], [], [], [], [], []
     alpha, coeff, norms, am = [], [], [], []
     po = ao = no = 0

@@ -15,7 +15,7 @@ from . import build as _build
 HFG_OK = 0
 FP64, MIXED = 0, 1
 NUM_CLASSES = 21
-FORM_AUTO, FORM_THREAD, FORM_WARP, FORM_GROUP = 0, 1, 2, 3
+FORM_AUTO, FORM_THREAD, FORM_WARP, FORM_GROUP, FORM_CHUNK = 0, 1, 2, 3, 4
 
 _lib = None
 
@@ -61,7 +61,7 @@ class ScfOptions(ctypes.Structure):
                 ("max_lshift_iter", ctypes.c_double), ("stop_lshift_thresh", ctypes.c_double),
                 ("schwartz_threshold", ctypes.c_double), ("density_threshold", ctypes.c_double),
                 ("precision", ctypes.c_int), ("fp32_cutoff", ctypes.c_double), ("full_rebuild_every", ctypes.c_int),
-                ("verbose", ctypes.c_int)]
+                ("verbose", ctypes.c_int), ("graph_iterations", ctypes.c_int), ("direct", ctypes.c_int)]
 
 
 class GradRequest(ctypes.Structure):
@@ -75,7 +75,8 @@ class ScfResult(ctypes.Structure):
     _fields_ = [("e_electronic", ctypes.c_double), ("e_nuclear", ctypes.c_double), ("e_total", ctypes.c_double),
                 ("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("delta_e", ctypes.c_double),
                 ("delta_d", ctypes.c_double), ("diis_error", ctypes.c_double), ("ms_total", ctypes.c_double),
-                ("ms_fock", ctypes.c_double), ("fock_builds", ctypes.c_int), ("s_squared", ctypes.c_double)]
+                ("ms_fock", ctypes.c_double), ("fock_builds", ctypes.c_int), ("s_squared", ctypes.c_double),
+                ("graph_replays", ctypes.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -107,6 +108,7 @@ def lib():
         L.hfg_set_primitive_threshold.argtypes = [vp, ctypes.c_double]
         L.hfg_set_graph_mode.argtypes = [vp, ip]
         L.hfg_set_precision_overlap.argtypes = [vp, ip, ctypes.c_double]
+        L.hfg_set_precision_shares.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.hfg_kernel_forms.argtypes = [vp, ip, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)]
         L.hfg_stream.argtypes = [vp]
         L.hfg_stream.restype = vp
@@ -123,6 +125,8 @@ def lib():
         L.hfg_measure_dmma_peak.argtypes = [ip, dpp]
         L.hfg_gradient.argtypes = [vp, ctypes.POINTER(GradRequest), dpp, dpp]
         L.hfg_boys_eval.argtypes = [ip, ip, ip, ctypes.c_longlong, dpp, dpp]
+        L.hfg_store_integrals.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ctypes.c_size_t)]
+        L.hfg_fock_conventional.argtypes = [vp, ctypes.POINTER(_Request), ctypes.POINTER(Stats)]
         _lib = L
     return _lib
 
@@ -227,6 +231,26 @@ class Engine:
             outs = [o.reshape(n, n, order="F") if o is not None else None for o in outs]
         return outs[0], outs[1], outs[2], st.as_dict()
 
+    def store_integrals(self, sthr=1e-10) -> int:
+        """Evaluate and keep every Schwartz-surviving integral (the DIRECT FALSE path); returns the bytes."""
+        b = ctypes.c_size_t()
+        self._check(lib().hfg_store_integrals(self.h, sthr, ctypes.byref(b)))
+        return b.value
+
+    def fock_conventional(self, D_tot, D_alpha, D_beta=None, sthr=1e-10):
+        """(J, Ka, Kb or None, stats) of the FULL densities from the stored integrals (host matrices)."""
+        uhf = D_beta is not None
+        flat = lambda x: np.asfortranarray(x, dtype=np.float64).ravel(order="F")
+        ins = [flat(D_tot), flat(D_alpha), flat(D_beta) if uhf else None]
+        outs = [np.zeros(ins[0].size) for _ in range(3 if uhf else 2)] + ([] if uhf else [None])
+        req = _Request(1 if uhf else 0, FP64, 0, sthr, 0.0, 0.0, *[x.ctypes.data if x is not None else None for x in ins],
+                       *[x.ctypes.data if x is not None else None for x in outs])
+        st = Stats()
+        self._check(lib().hfg_fock_conventional(self.h, ctypes.byref(req), ctypes.byref(st)))
+        n = self.nao
+        outs = [o.reshape(n, n, order="F") if o is not None else None for o in outs]
+        return outs[0], outs[1], outs[2], st.as_dict()
+
     def fock_device(self, ptrs: dict, unrestricted=False, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-4):
         """Same on device pointers (ints): keys dD_tot, dD_alpha, dD_beta, J, K_alpha, K_beta."""
         g = lambda k: ptrs.get(k) or None
@@ -241,6 +265,10 @@ class Engine:
         resident blocks per SM)."""
         self._check(lib().hfg_set_precision_overlap(self.h, 1 if on else 0, float(share)))
 
+    def set_precision_shares(self, share_fp64: float, share_fp32: float):
+        """Grid limits of the overlapped FP64 and FP32 class kernels, separately."""
+        self._check(lib().hfg_set_precision_shares(self.h, float(share_fp64), float(share_fp32)))
+
     def set_graph_mode(self, on: bool):
         """Replay device-pointer Fock builds as CUDA graphs (captured on first use per request key)."""
         self._check(lib().hfg_set_graph_mode(self.h, 1 if on else 0))
@@ -250,7 +278,7 @@ class Engine:
         self._check(lib().hfg_set_primitive_threshold(self.h, float(threshold)))
 
     def set_kernel_form(self, form, qclass=-1, fp32=False):
-        """Force a kernel form (FORM_THREAD / FORM_WARP / FORM_GROUP) or return to FORM_AUTO."""
+        """Force a kernel form (FORM_THREAD / FORM_WARP / FORM_GROUP / FORM_CHUNK) or return to FORM_AUTO."""
         self._check(lib().hfg_set_kernel_form(self.h, qclass, 1 if fp32 else 0, form))
 
     def kernel_forms(self, fp32=False, unrestricted=False):

@@ -95,9 +95,6 @@ def check_supported(job: JobInput, input_frame: bool = False) -> None:
                          "frame (src/Molecule.cpp:19-27), which this engine does not do: set SYMMETRY FALSE in "
                          "$scf, or run with input_frame=True to compute in the input frame (same energy; "
                          "densities and gradients in the input frame)")
-    if not job.scf.get("direct", True):
-        raise ValueError("DIRECT FALSE (the reference's stored-integral SCF, src/SCF.cpp:233-521) is not "
-                         "available in this engine: set DIRECT TRUE")
 
 
 def scf_options(job: JobInput, precision: int = 0, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0) -> dict:
@@ -113,4 +110,4 @@ def scf_options(job: JobInput, precision: int = 0, fp32_cutoff: float = 1e-4, fu
         lshift_gap_tol=s.get("lshift_gap_tol", float("inf")), max_lshift_iter=float(s.get("max_lshift_cycles", max_iter)),
         stop_lshift_thresh=s.get("stop_lshift_thresh", 0.0), schwartz_threshold=s.get("schwartz_thresh", 1e-10),
         density_threshold=s.get("density_thresh", 1e-10), precision=precision, fp32_cutoff=fp32_cutoff,
-        full_rebuild_every=full_rebuild_every, verbose=0)
+        full_rebuild_every=full_rebuild_every, verbose=0, direct=int(s.get("direct", True)))

@@ -131,6 +131,18 @@ int hfg_set_primitive_threshold(hfg_engine* engine, double threshold);
 /* SCF::buildFockMatrixDirect (include/SCF.hpp:129, src/SCF.cpp:523-744); `stats` may be NULL. */
 int hfg_fock_direct(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_stats* stats);
 
+/* IntegralEngine::electronRepulsionTensor (src/IntegralEngine.cpp:635-692), the stored-integral (DIRECT
+ * FALSE) path: evaluates every shell quartet whose Schwartz product reaches `schwartz_threshold` once, in
+ * FP64, and keeps the integral blocks in device memory (`bytes`, may be NULL, receives their size).  Fails
+ * with HFG_ERR_NOMEM when they would need more than 80% of the free device memory. */
+int hfg_store_integrals(hfg_engine* engine, double schwartz_threshold, size_t* bytes);
+
+/* SCF::buildFockMatrix (src/SCF.cpp:233-521): J[D] and K[D] of the FULL densities from the stored
+ * integrals (the request's dD_tot / dD_alpha / dD_beta carry D_tot, D_alpha, D_beta here), with the
+ * reference's AO-level skip |(ij|kl)| < schwartz_threshold; the caller forms F = h + J - K as SCF.cpp:507-520
+ * does.  Needs hfg_store_integrals first; `precision` and the density threshold are not used. */
+int hfg_fock_conventional(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_stats* stats);
+
 /* Kernel forms of a class kernel.  THREAD: one thread per shell quartet.  WARP: one warp per quartet
  * (the large d classes).  GROUP: a power-of-two group of lanes per quartet, splitting its primitive
  * quartets (the small contracted classes, L <= 3).  AUTO: on the first build that runs the class with
@@ -141,6 +153,7 @@ int hfg_fock_direct(hfg_engine* engine, const hfg_fock_request* req, hfg_fock_st
 #define HFG_FORM_THREAD 1
 #define HFG_FORM_WARP 2
 #define HFG_FORM_GROUP 3
+#define HFG_FORM_CHUNK 4 /* one thread per (quartet, chunk of ket Cartesian components): the FP32 d classes */
 /* Set the form of class `qclass` (-1: every class) at precision `fp32` (0: FP64 kernels, 1: FP32
  * kernels).  HFG_FORM_AUTO forgets earlier timings; a form the class was not compiled in returns
  * HFG_ERR_UNSUPPORTED (with qclass -1 such classes keep AUTO). */
@@ -150,6 +163,10 @@ int hfg_set_kernel_form(hfg_engine* engine, int qclass, int fp32, int form);
  * the FP32 / memory-latency bound kernels share the SMs.  On by default with share 1 (full grids).  No
  * reference counterpart. */
 int hfg_set_precision_overlap(hfg_engine* engine, int on, double share);
+/* The same limit set separately for the FP64 and the FP32 class kernels' grids (each in (0, 1]): the FP64
+ * kernels keep the FP64 pipe busy with few warps per SM, so a smaller FP64 share leaves the rest of the SM
+ * to the FP32 kernels running beside them.  No reference counterpart. */
+int hfg_set_precision_shares(hfg_engine* engine, double share_fp64, double share_fp32);
 
 /* CUDA-graph replay of Fock builds (no reference counterpart; the SCF driver calls hfg_fock_direct on
  * device pointers every iteration).  On: a device-pointer request runs eagerly once and is captured
@@ -223,6 +240,12 @@ typedef struct hfg_scf_options
     double fp32_cutoff;        /* FP32 cutoff of the mixed mode (1e-4) */
     int full_rebuild_every;    /* 0: incremental builds as the reference; k > 0: full build every k iterations */
     int verbose;               /* print the iteration table to stdout */
+    int graph_iterations;      /* 1: run every SCF iteration after the first as one replayed CUDA graph (Fock build,
+                                  DIIS on the device, orbital step, energy and convergence measures; one host
+                                  read-back per iteration).  Used when damping and level shifting are off and
+                                  DIIS_SIZE <= 16; otherwise, or if the capture is refused, iterations run eagerly. */
+    int direct;                /* DIRECT (1).  0: the stored-integral SCF (SCF.cpp:233-521): integrals stored once by
+                                  hfg_store_integrals, every Fock build F = h + J[D] - K[D] from them */
 } hfg_scf_options;
 
 typedef struct hfg_scf_result
@@ -235,6 +258,7 @@ typedef struct hfg_scf_result
     double ms_fock;  /* device time of the Fock builds */
     int fock_builds;
     double s_squared; /* <S^2> (UHF) */
+    int graph_replays; /* iterations that ran as a replayed CUDA graph (graph_iterations) */
 } hfg_scf_result;
 
 /* The reference's defaults (SCF.hpp:9-32, Input.cpp:127-140) for a molecule of this multiplicity. */

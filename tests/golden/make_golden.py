@@ -31,6 +31,9 @@ SYSTEMS = {
     "w2_ccpvdz": (lambda: w.water_lattice(2, 1, 1), "cc-pVDZ", 0, 1, {}),
     "w4_631gss": (lambda: w.water_lattice(2, 2, 1), "6-31G**", 0, 1, {}),
     "w2_cation_uhf_631gss": (lambda: w.water_lattice(2, 1, 1), "6-31G**", 1, 2, dict(GUESS_MIX=2)),
+    # The stored-integral SCF (DIRECT FALSE: SCF::buildFockMatrix from electronRepulsionTensor).
+    "h2o_631g_conv": (w.monomer, "6-31G", 0, 1, dict(DIRECT=False)),
+    "w2_ccpvdz_conv": (lambda: w.water_lattice(2, 1, 1), "cc-pVDZ", 0, 1, dict(DIRECT=False)),
 }
 
 
@@ -41,7 +44,7 @@ def make(name, spec, run_scf=True):
     kw.update(TIGHT)
     kw.update(extra)
     text = w.input_text(Z, xyz, basis, charge=charge, multiplicity=mult, **kw)
-    s = ref.RefSession(text)
+    s = ref.RefSession(text.replace("DIRECT             FALSE", "DIRECT             TRUE"))
     soa = s.basis_soa()
     Q = s.schwartz()
     Da, Db = s.guess()
@@ -57,6 +60,11 @@ def make(name, spec, run_scf=True):
                nuclear_repulsion=s.nuclear_repulsion, Q=Q, Da=Da, Db=Db, Fa=Fa, Fb=Fb, Da2=Da2, Db2=Db2, Fa2=Fa2,
                Fb2=Fb2, S=S, T=T, V=V, **{"soa_" + k: v for k, v in soa.items()})
     if run_scf:
+        if extra.get("DIRECT", True) is False:
+            # The reference's direct-build entry points need the direct set-up: the matrices above come
+            # from a DIRECT TRUE session of the same input; the SCF runs with the stored integrals.
+            s.close()
+            s = ref.RefSession(text)
         r = s.scf_run()
         out.update(e_elec=r["e_elec"], e_nuc=r["e_nuc"], scf_iterations=r["iterations"], Da_scf=r["Da"],
                    Db_scf=r["Db"])

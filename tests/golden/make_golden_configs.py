@@ -8,7 +8,7 @@
   the incremental build from the guess to the converged density (F_inc = F + J[dD] - K[dD],
   SCF.cpp:731-743).  The wall time of the reference's full Fock build is recorded as well
   (``ref_fock_s``, ``ref_threads``), for the calibration of the C restatement against it.
-* ``fd_w8_ccpvdz``: (H2O)_8 on a 2x2x2 lattice, RHF/cc-pVDZ (144 basis functions under the reference's
+* ``cfg_fd_w8_ccpvdz``: (H2O)_8 on a 2x2x2 lattice, RHF/cc-pVDZ (144 basis functions under the reference's
   basis reader).  Central differences (+-1e-4 bohr) of the reference's total energy for nine Cartesian
   coordinates (``coords``: atom, axis) -- the three axes of three atoms in different waters.  One
   reference SCF at this size takes ~4.5 minutes on 8 cores, so the full 72-coordinate gradient (145
@@ -77,14 +77,14 @@ def fd_energy(Z, xyz):
 
 def make_fd_w8():
     Z, xyz0 = w.water_lattice(2, 2, 2)
-    path = os.path.join(HERE, "fd_w8_ccpvdz.npz")
+    path = os.path.join(HERE, "cfg_fd_w8_ccpvdz.npz")
     g = np.full(len(FD_COORDS), np.nan)
     for k, (a, ax) in enumerate(FD_COORDS):
         xp, xm = xyz0.copy(), xyz0.copy()
         xp[a, ax] += FD_STEP
         xm[a, ax] -= FD_STEP
         g[k] = (fd_energy(Z, xp) - fd_energy(Z, xm)) / (2 * FD_STEP)
-        print(f"fd_w8_ccpvdz: atom {a} axis {ax} dE/dx = {g[k]:.9f}", flush=True)
+        print(f"cfg_fd_w8_ccpvdz: atom {a} axis {ax} dE/dx = {g[k]:.9f}", flush=True)
         # Written after every coordinate, so that an interrupted run keeps what it has (NaN = not yet).
         np.savez_compressed(path, Z=np.array(Z, np.int32), xyz=xyz0, basis=np.array("cc-pVDZ"), charge=0,
                             multiplicity=1, coords=np.array(FD_COORDS, np.int32), grad_fd=g, step=FD_STEP,

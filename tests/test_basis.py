@@ -35,3 +35,19 @@ def test_workload_coordinates_roundtrip_through_input_text():
     rows = [l.split() for l in text.splitlines() if l.strip()[:1] in ("H", "O")]
     parsed = np.array([[float(v) for v in r[1:4]] for r in rows])
     assert np.array_equal(parsed, x)
+
+
+def test_general_contractions_opt_in():
+    """Opt-in extension: one shell per coefficient row of a generally contracted shell (cc-pVDZ); the
+    default keeps the reference's first-row rule, and segmented sets (6-31G**) are unchanged."""
+    from hfgpu import basis, workloads
+
+    Z, xyz = workloads.monomer()
+    ref = basis.pack("cc-pVDZ", Z, xyz)
+    gen = basis.pack("cc-pVDZ", Z, xyz, general_contractions=True)
+    nbf = lambda s: int(sum((l + 1) * (l + 2) // 2 for l in s["l"]))
+    assert nbf(ref) == 18 and nbf(gen) == 25  # O 3s2p1d + H 2s1p each, Cartesian d
+    assert np.all(gen["coeff"] != 0.0)
+    seg = basis.pack("6-31G**", Z, xyz, general_contractions=True)
+    seg0 = basis.pack("6-31G**", Z, xyz)
+    assert all(np.array_equal(seg[k], seg0[k]) for k in seg)

@@ -2,8 +2,10 @@
 only ever picks a compiled form.
 
 Forms: THREAD (one thread per shell quartet), WARP (one warp per quartet, large d classes), GROUP (a
-power-of-two lane group per quartet splitting its primitive quartets, classes up to L = 3).  Tolerances
-as in test_gpu_fock: FP64 within 1e-10 Eh of the reference, mixed within 1e-6 of FP64.
+power-of-two lane group per quartet splitting its primitive quartets, classes up to L = 3), CHUNK (one
+thread per quartet and chunk of ket components, FP32 d classes).  Tolerances as in test_gpu_fock: FP64
+within 1e-10 Eh of the reference, mixed within 1e-6 of FP64; with every quartet in FP32, two FP32 forms
+within 1e-5 of each other and of FP64 (FP32 integrals carry ~1e-7 relative error, J/K elements are O(10)).
 """
 import numpy as np
 import pytest
@@ -79,6 +81,35 @@ def test_gpu_forced_group_form_mixed_close_to_fp64(name):
     assert any(f == 3 for f in s32["form_fp32"])
     assert np.max(np.abs(J32 - J64)) <= 1e-6
     assert np.max(np.abs(K32 - K64)) <= 1e-6
+
+
+def _chunk_else_default(mask):
+    from hfgpu.engine import FORM_CHUNK
+
+    return FORM_CHUNK if mask >> FORM_CHUNK & 1 else None
+
+
+@pytest.mark.parametrize("name", ["w2_631gss", "w2_cation_uhf_631gss", "w2_ccpvdz"])
+def test_gpu_forced_chunk_form_fp32(name):
+    g = load_golden(name)
+    e = _engine(g)
+    uhf = bool(g["unrestricted"])
+    Da, Db = g["Da"], g["Db"]
+    args = (Da + Db, Da, Db if uhf else None)
+    J64, K64, _, _ = e.fock(*args)
+    every = dict(precision=1, fp32_cutoff=1e30)  # every surviving quartet in FP32
+    _force(e, True, _non_group)
+    J1, K1, _, s1 = e.fock(*args, **every)
+    _force(e, True, _chunk_else_default)
+    J2, K2, _, s2 = e.fock(*args, **every)
+    chunked = [qc for qc, n in enumerate(s2["quartets_fp32"]) if n and s2["form_fp32"][qc] == 4]
+    assert len(chunked) >= 4, s2["form_fp32"]
+    assert sum(s2["quartets_fp64"]) == 0
+    assert np.max(np.abs(J2 - J1)) <= 1e-5 and np.max(np.abs(K2 - K1)) <= 1e-5
+    assert np.max(np.abs(J2 - J64)) <= 1e-5 and np.max(np.abs(K2 - K64)) <= 1e-5
+    # At the default cutoff, as the mixed build runs.
+    J3, K3, _, _ = e.fock(*args, precision=1, fp32_cutoff=1e-4)
+    assert np.max(np.abs(J3 - J64)) <= 1e-6 and np.max(np.abs(K3 - K64)) <= 1e-6
 
 
 def test_gpu_autotune_picks_compiled_forms():

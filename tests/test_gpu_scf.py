@@ -1,6 +1,6 @@
 """End-to-end direct SCF with the GPU Fock build against the reference's converged energies
 (golden fixtures from SCF::run, converged to ENERGY_TOL 1e-10): |E_gpu - E_ref| <= 1e-9 Eh on the FP64
-path; the mixed FP32/FP64 path within 1e-6 Eh of the FP64 GPU energy."""
+path; the mixed FP32/FP64 path, at the shipped default FP32 cutoff (1e-4), within 1e-6 Eh of the FP64 GPU energy."""
 import numpy as np
 import pytest
 
@@ -28,7 +28,7 @@ def test_gpu_scf_mixed_energy_close_to_fp64(name):
 
     g = load_golden(name)
     r64, _, _, _ = run_input(str(g["input_text"]))
-    r32, _, _, _ = run_input(str(g["input_text"]), precision=1, fp32_cutoff=1e-6)
+    r32, _, _, _ = run_input(str(g["input_text"]), precision=1)  # the default fp32_cutoff, 1e-4
     assert r32["converged"] == 1
     assert abs(r32["e_total"] - r64["e_total"]) <= 1e-6
 
@@ -40,3 +40,28 @@ def test_gpu_core_guess_matches_reference():
     e = Engine(g["soa"])
     Da, Db = e.core_guess(g["Z"], g["xyz"], 0, 1)
     assert np.max(np.abs(Da - g["Da"])) <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["h2o_631g", "w4_631gss", "w2_cation_uhf_631gss"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_gpu_scf_graph_iterations_match_reference(name, precision):
+    """Every iteration after the first replays one captured CUDA graph (Fock build, DIIS on the device,
+    orbital step, measures): the FP64 energy within 1e-9 Eh of the reference, mixed within 1e-6."""
+    from hfgpu import inputs
+    from hfgpu.engine import Engine
+
+    g = load_golden(name)
+    job = inputs.parse(str(g["input_text"]))
+    opts = inputs.scf_options(job, precision=precision)
+    opts["graph_iterations"] = 1
+    e = Engine(g["soa"])
+    res, Da, Db = e.scf(job.Z, job.xyz, job.charge, job.multiplicity, opts)
+    assert res["converged"] == 1
+    assert res["graph_replays"] == res["iterations"] - 1, (res["graph_replays"], res["iterations"])
+    e_ref = float(g["e_elec"] + g["e_nuc"])
+    assert abs(res["e_total"] - e_ref) <= (1e-9 if precision == 0 else 1e-6)
+    # Same densities as the eager path.
+    opts["graph_iterations"] = 0
+    r0, Da0, Db0 = Engine(g["soa"]).scf(job.Z, job.xyz, job.charge, job.multiplicity, opts)
+    assert res["graph_replays"] >= 0 and r0["graph_replays"] == 0
+    assert np.max(np.abs(Da - Da0)) <= (1e-6 if precision == 0 else 1e-5)  # both converged to DENSITY_TOL 1e-7

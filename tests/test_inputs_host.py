@@ -56,12 +56,13 @@ def test_symmetry_true_is_rejected_not_ignored():
     inputs.check_supported(inputs.parse(_MIN.format(scf="SYMMETRY FALSE\n")))
 
 
-def test_direct_false_is_rejected_not_ignored():
+def test_direct_false_selects_the_stored_integral_scf():
     from hfgpu import inputs
 
     job = inputs.parse(_MIN.format(scf="SYMMETRY FALSE\nDIRECT FALSE\n"))
-    with pytest.raises(ValueError, match="DIRECT"):
-        inputs.check_supported(job)
+    inputs.check_supported(job)
+    assert inputs.scf_options(job)["direct"] == 0
+    assert inputs.scf_options(inputs.parse(_MIN.format(scf="SYMMETRY FALSE\n")))["direct"] == 1
 
 
 @pytest.mark.parametrize("name", ["h2o_631g", "w2_631gss", "w2_ccpvdz"])
