@@ -19,9 +19,10 @@ SCHWARTZ_THRESH = DENSITY_THRESH = 1e-10.  A step = one hfg_fock_direct call.
              gradient, --no-scf skips them.
 * cpu_baseline / --impl reference   the C restatement of the reference's OpenMP build (oracle/, built
              with the reference's release flags) on this host's cores.  A CPU step is the build over a
-             seeded sample of bra shell pairs: its wall time is measured (ms_per_step) and its Fock builds/s
-             is the fraction of the build's surviving shell quartets it held over that time;
-             --cpu-full also times one unsampled build to check that scaling.
+             seeded sample of the ordered bra shell pairs of the reference's nShells^4 loop (each sampled
+             bra scans its whole ket range): its wall time is measured (ms_per_step) and its Fock builds/s
+             is the sampled fraction of the loop over that time; --cpu-full also times one unsampled
+             build to check that scaling.
 
 Multi-GPU (torchrun): every rank builds the same workload on its own GPU (independent replicas, no
 collective on the data path; weak scaling).
@@ -200,10 +201,11 @@ class CpuBuild:
     """The reference's direct Fock build on the host cores: the C restatement of SCF::buildFockMatrixDirect
     (oracle/hf_oracle.c, OpenMP over all host threads) built with the reference's release flags.
 
-    One step runs the build over a seeded random sample of bra shell pairs (SCF.cpp's outer loop), so that a
-    step takes seconds instead of the minutes of a full build.  Its throughput in Fock builds/s is the
-    measured wall time of the step scaled by the fraction of the build's surviving shell quartets the
-    sample held; ``full()`` times one unsampled build for the check of that scaling."""
+    One step runs the build over a seeded random sample of the ordered bra shell pairs (a, b) of the
+    reference's nShells^4 loop (SCF.cpp:592-600), scanning each sampled bra's whole ket range with the same
+    skip tests, so that a step takes seconds instead of the minutes of a full build and a fraction f of the
+    bras costs f of the build, scan included.  Its throughput in Fock builds/s is f over the measured wall
+    time of the step; ``full()`` times one unsampled build for the check of that scaling."""
 
     def __init__(self, soa, Z, xyz, Da, total_quartets=None):
         from oracle import port
@@ -215,7 +217,7 @@ class CpuBuild:
         self.dt, self.da = 2.0 * Da, Da
         self.total = int(total_quartets if total_quartets is not None else self.B.count_survivors(self.Q, self.dt, self.da))
         ns = self.B.nshells
-        self.npairs = ns * (ns + 1) // 2
+        self.npairs = ns * ns  # ordered bra pairs of the nShells^4 loop
 
     def sample(self, frac, seed):
         import numpy as np
@@ -224,8 +226,9 @@ class CpuBuild:
         t0 = time.perf_counter()
         _, _, _, n = self.B.fock_direct_sample(self.Q, self.dt, self.da, mask)
         t = time.perf_counter() - t0
-        return {"seconds": t, "quartets": int(n), "bra_pairs": int(mask.sum()), "fraction": n / max(self.total, 1),
-                "builds_per_s": (n / max(self.total, 1)) / t if t > 0 else 0.0}
+        f = int(mask.sum()) / self.npairs
+        return {"seconds": t, "quartets": int(n), "bra_pairs": int(mask.sum()), "fraction": f,
+                "quartet_fraction": n / max(self.total, 1), "builds_per_s": f / t if t > 0 else 0.0}
 
     def calibrate(self, target_s, seed=12345):
         """Sampling fraction whose step takes about target_s seconds."""
@@ -248,9 +251,9 @@ def cpu_baseline(soa, Z, xyz, Da, target_s: float, total_quartets: int | None = 
     cb = CpuBuild(soa, Z, xyz, Da, total_quartets)
     r = cb.sample(cb.calibrate(target_s), seed=0)
     return {"value": r["builds_per_s"], "unit": "Fock builds/s", "cores": cb.cores, "kind": "port",
-            "sample": (f"{r['bra_pairs']} of {cb.npairs} bra shell pairs (seeded), {r['quartets']} of {cb.total} "
-                       f"surviving quartets ({100 * r['fraction']:.3f}% of the build) in {r['seconds']:.2f} s measured; "
-                       f"builds/s = sampled fraction / measured seconds"),
+            "sample": (f"{r['bra_pairs']} of {cb.npairs} ordered bra shell pairs (seeded, {100 * r['fraction']:.3f}% of "
+                       f"the build's loop; {r['quartets']} of {cb.total} surviving quartets) in {r['seconds']:.2f} s "
+                       f"measured; builds/s = sampled fraction / measured seconds"),
             "build": "oracle/hf_oracle.c with the reference's release flags (Makefile:47, without -march=native/-flto)"}
 
 
@@ -276,6 +279,7 @@ def reference_arm(args, dist):
         "config": {"workload": WORKLOADS[args.workload]["name"], "precision": "fp64 (reference algorithm)",
                    "step": "the direct build over a seeded random sample of bra shell pairs"},
         "sampling": {"fraction_of_build_per_step": statistics.median(r["fraction"] for r in runs),
+                     "quartet_fraction_per_step": statistics.median(r["quartet_fraction"] for r in runs),
                      "quartets_per_step": int(statistics.median(r["quartets"] for r in runs)),
                      "total_quartets": cb.total, "extrapolated_builds_per_s": value,
                      "extrapolated_ms_per_full_build": 1000.0 / value if value else None},

@@ -22,6 +22,7 @@
 #include "engine.h"
 #include "eri_grad.cuh"
 #include "hfgpu.h"
+#include "onee.h"
 
 #include <algorithm>
 #include <array>
@@ -173,6 +174,17 @@ struct hfg_engine
     bool have_gtab = false;
     hfg::DevBuf<int> d_shell_atom;
     hfg::DevBuf<double> d_grad;
+    // One-electron integrals on the device (molecule 0): the basis arrays, the shell pairs per pair class
+    // (oriented l1 >= l2), the nuclei, and scratch for W.
+    bool have_onee = false;
+    hfg::DevBuf<int> d_ob_int;    // l, nprim, prim_off, ao_off, norm_off (nshells each)
+    hfg::DevBuf<double> d_ob_dbl; // centers (3 nshells), alpha, coeff, norms
+    hfg::DevBuf<int2> d_ob_pairs[hfg::kNumPairClasses];
+    int ob_npairs[hfg::kNumPairClasses] {};
+    hfg::OneeBasis ob {};
+    hfg::DevBuf<double4> d_nuc;
+    hfg::DevBuf<double> d_W;
+    hfg::DevBuf<int> d_shell_atom1;
     // Final state of the last hfg_scf_run (for hfg_gradient's backward call).
     std::vector<double> scf_Da, scf_Db, scf_W;
     bool scf_valid = false, scf_uhf = false;
@@ -1715,6 +1727,125 @@ static void fock_conventional(hfg_engine* e, const hfg_fock_request& r, hfg_fock
     }
 }
 
+// Device copies of molecule 0's basis and its shell pairs per pair class (once per engine).
+static void upload_onee(hfg_engine* e)
+{
+    if (e->have_onee)
+        return;
+    if (e->nmol != 1)
+        throw HfgError(HFG_ERR_INVALID, "one-electron integrals: the engine must hold exactly one molecule");
+    const HostBasis& b = e->basis[0];
+    const int ns       = static_cast<int>(b.l.size());
+    std::vector<int> ints;
+    for (const auto* v : {&b.l, &b.nprim, &b.prim_off, &b.ao_off, &b.norm_off}) ints.insert(ints.end(), v->begin(), v->end());
+    std::vector<double> dbl;
+    for (const auto* v : {&b.centers, &b.alpha, &b.coeff, &b.norms}) dbl.insert(dbl.end(), v->begin(), v->end());
+    e->d_ob_int.upload(ints, e->stream);
+    e->d_ob_dbl.upload(dbl, e->stream);
+    const int* ip    = e->d_ob_int.p;
+    const double* dp = e->d_ob_dbl.p;
+    e->ob = OneeBasis {ip, ip + ns, ip + 2 * ns, ip + 3 * ns, ip + 4 * ns, dp, dp + 3 * ns, dp + 3 * ns + b.alpha.size(),
+                       dp + 3 * ns + b.alpha.size() + b.coeff.size()};
+    std::vector<std::vector<int2>> cls(kNumPairClasses);
+    for (int s1 = 0; s1 < ns; ++s1)
+        for (int s2 = 0; s2 <= s1; ++s2)
+        {
+            int a = s1, c = s2;
+            if (b.l[c] > b.l[a])
+                std::swap(a, c);
+            cls[pair_class(b.l[a], b.l[c])].push_back(make_int2(a, c));
+        }
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        e->d_ob_pairs[pc].upload(cls[pc], e->stream);
+        e->ob_npairs[pc] = static_cast<int>(cls[pc].size());
+    }
+    HFG_CUDA(cudaStreamSynchronize(e->stream)); // the host vectors die here
+    e->have_onee = true;
+}
+
+static void upload_nuclei(hfg_engine* e, int natom, const int* Z, const double* xyz)
+{
+    std::vector<double4> nuc(natom);
+    for (int a = 0; a < natom; ++a) nuc[a] = make_double4(xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2], static_cast<double>(Z[a]));
+    e->d_nuc.upload(nuc, e->stream);
+    HFG_CUDA(cudaStreamSynchronize(e->stream)); // the host vector dies here
+}
+
+// IntegralEngine::overlapMatrix / kineticMatrix / nuclearAttractionMatrix (src/IntegralEngine.cpp:78-368) on
+// the device: S, T, V (n x n column-major, device pointers), FP64.
+void one_electron_device(hfg_engine* e, int natom, const int* Z, const double* xyz, double* S, double* T, double* V)
+{
+    upload_onee(e);
+    upload_nuclei(e, natom, Z, xyz);
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        OneeLaunch L {};
+        L.pairs      = e->d_ob_pairs[pc].p;
+        L.npairs     = e->ob_npairs[pc];
+        L.basis      = e->ob;
+        L.nuc        = e->d_nuc.p;
+        L.natom      = natom;
+        L.n          = e->mols[0].nao;
+        L.boys_slice = e->d_boys64[pair_class_l1(pc) + pair_class_l2(pc)].p;
+        L.S          = S;
+        L.T          = T;
+        L.V          = V;
+        L.stream     = e->stream;
+        L.num_sms    = e->num_sms;
+        HFG_CUDA(launch_one_electron(pc, L));
+    }
+}
+
+// One-electron part of the gradient on the device: sum D d(T + V)/dX - W dS/dX added into the device array
+// grad (natom x 3); D (total density) and W (energy-weighted density) are device pointers.
+static void gradient_one_electron_device(hfg_engine* e, const std::vector<int>& shell_atom, int natom, const int* Z,
+                                         const double* xyz, const double* D, const double* W, double* grad)
+{
+    upload_onee(e);
+    upload_nuclei(e, natom, Z, xyz);
+    e->d_shell_atom1.upload(shell_atom, e->stream);
+    for (int pc = 0; pc < kNumPairClasses; ++pc)
+    {
+        OneeLaunch L {};
+        L.pairs      = e->d_ob_pairs[pc].p;
+        L.npairs     = e->ob_npairs[pc];
+        L.basis      = e->ob;
+        L.nuc        = e->d_nuc.p;
+        L.natom      = natom;
+        L.n          = e->mols[0].nao;
+        L.boys_slice = e->d_boys64[pair_class_l1(pc) + pair_class_l2(pc) + 2].p;
+        L.D          = D;
+        L.W          = W;
+        L.shell_atom = e->d_shell_atom1.p;
+        L.grad       = grad;
+        L.stream     = e->stream;
+        L.num_sms    = e->num_sms;
+        HFG_CUDA(launch_one_electron_grad(pc, L));
+    }
+    HFG_CUDA(cudaStreamSynchronize(e->stream)); // shell_atom belongs to the caller
+}
+
+// Shell -> atom from the shell centres (a shell sits on the nucleus with the same coordinates).
+static std::vector<int> shell_atoms(const hfg_engine* e, int natom, const double* xyz)
+{
+    const auto& hb = e->basis[0];
+    std::vector<int> shell_atom(hb.l.size(), -1);
+    for (size_t sh = 0; sh < hb.l.size(); ++sh)
+    {
+        for (int a = 0; a < natom; ++a)
+            if (hb.centers[3 * sh] == xyz[3 * a] && hb.centers[3 * sh + 1] == xyz[3 * a + 1] &&
+                hb.centers[3 * sh + 2] == xyz[3 * a + 2])
+            {
+                shell_atom[sh] = a;
+                break;
+            }
+        if (shell_atom[sh] < 0)
+            throw HfgError(HFG_ERR_INVALID, "gradient: a shell centre matches no nucleus");
+    }
+    return shell_atom;
+}
+
 const hfg_basis* engine_basis(const hfg_engine* e)
 {
     return (e && e->nmol == 1) ? &e->basis[0].view : nullptr;
@@ -2393,21 +2524,7 @@ int hfg_gradient(hfg_engine* e, const hfg_gradient_request* r, double* grad, dou
         const double* W  = use_last ? e->scf_W.data() : r->W;
         if (!Db || !W)
             throw HfgError(HFG_ERR_INVALID, "hfg_gradient: missing D_beta or W");
-        // Shell -> atom from the shell centres.
-        const auto& hb = e->basis[0];
-        std::vector<int> shell_atom(hb.l.size(), -1);
-        for (size_t sh = 0; sh < hb.l.size(); ++sh)
-        {
-            for (int a = 0; a < r->natom; ++a)
-                if (hb.centers[3 * sh] == r->xyz[3 * a] && hb.centers[3 * sh + 1] == r->xyz[3 * a + 1] &&
-                    hb.centers[3 * sh + 2] == r->xyz[3 * a + 2])
-                {
-                    shell_atom[sh] = a;
-                    break;
-                }
-            if (shell_atom[sh] < 0)
-                throw HfgError(HFG_ERR_INVALID, "hfg_gradient: a shell centre matches no nucleus");
-        }
+        const std::vector<int> shell_atom = hfg::shell_atoms(e, r->natom, r->xyz);
         std::vector<double> Dt(N2);
         for (size_t k = 0; k < N2; ++k) Dt[k] = Da[k] + Db[k];
         for (int k = 0; k < 3; ++k)
@@ -2430,9 +2547,74 @@ int hfg_gradient(hfg_engine* e, const hfg_gradient_request* r, double* grad, dou
         if (ms_two_electron)
             *ms_two_electron = ms;
         e->last_valid = false; // the lists now hold the gradient's quartets
-        const int rc = hfg_gradient_one_electron(&hb.view, shell_atom.data(), r->natom, r->Z, r->xyz, Dt.data(), W, grad);
-        if (rc != HFG_OK)
-            throw HfgError(rc, "hfg_gradient: one-electron part failed");
+        // Nuclear repulsion (src/Molecule.cpp:80-89 differentiated) on the host; the one-electron and overlap
+        // parts on the device, with the total density still in d_dD[0].
+        const int na = r->natom;
+        for (int i = 0; i < na; ++i)
+            for (int j = 0; j < na; ++j)
+            {
+                if (i == j)
+                    continue;
+                double d[3], r2 = 0.0;
+                for (int k = 0; k < 3; ++k)
+                {
+                    d[k] = r->xyz[3 * i + k] - r->xyz[3 * j + k];
+                    r2 += d[k] * d[k];
+                }
+                const double f = static_cast<double>(r->Z[i] * r->Z[j]) / (r2 * std::sqrt(r2));
+                for (int k = 0; k < 3; ++k) grad[3 * i + k] -= f * d[k];
+            }
+        e->d_W.alloc(N2);
+        HFG_CUDA(cudaMemcpyAsync(e->d_W.p, W, sizeof(double) * N2, cudaMemcpyHostToDevice, e->stream));
+        HFG_CUDA(cudaMemsetAsync(e->d_grad.p, 0, sizeof(double) * 3 * na, e->stream));
+        hfg::gradient_one_electron_device(e, shell_atom, na, r->Z, r->xyz, e->d_dD[0].p, e->d_W.p, e->d_grad.p);
+        std::vector<double> g1(static_cast<size_t>(3) * na);
+        HFG_CUDA(cudaMemcpyAsync(g1.data(), e->d_grad.p, sizeof(double) * g1.size(), cudaMemcpyDeviceToHost, e->stream));
+        HFG_CUDA(cudaStreamSynchronize(e->stream));
+        for (size_t k = 0; k < g1.size(); ++k) grad[k] += g1[k];
+    });
+}
+
+int hfg_one_electron_gpu(hfg_engine* e, int natom, const int* Z, const double* xyz, double* S, double* T, double* V)
+{
+    if (!e || natom <= 0 || !Z || !xyz || !S || !T || !V)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        if (e->nmol != 1)
+            throw HfgError(HFG_ERR_INVALID, "hfg_one_electron_gpu: the engine must hold exactly one molecule");
+        const size_t N2 = static_cast<size_t>(e->mols[0].nao) * e->mols[0].nao;
+        hfg::DevBuf<double> d;
+        d.alloc(3 * N2);
+        hfg::one_electron_device(e, natom, Z, xyz, d.p, d.p + N2, d.p + 2 * N2);
+        HFG_CUDA(cudaMemcpyAsync(S, d.p, sizeof(double) * N2, cudaMemcpyDeviceToHost, e->stream));
+        HFG_CUDA(cudaMemcpyAsync(T, d.p + N2, sizeof(double) * N2, cudaMemcpyDeviceToHost, e->stream));
+        HFG_CUDA(cudaMemcpyAsync(V, d.p + 2 * N2, sizeof(double) * N2, cudaMemcpyDeviceToHost, e->stream));
+        HFG_CUDA(cudaStreamSynchronize(e->stream));
+    });
+}
+
+int hfg_gradient_one_electron_gpu(hfg_engine* e, int natom, const int* Z, const double* xyz, const double* D,
+                                  const double* W, double* grad)
+{
+    if (!e || natom <= 0 || !Z || !xyz || !D || !W || !grad)
+        return HFG_ERR_INVALID;
+    return guarded(e, [&] {
+        HFG_CUDA(cudaSetDevice(e->device));
+        if (e->nmol != 1)
+            throw HfgError(HFG_ERR_INVALID, "hfg_gradient_one_electron_gpu: the engine must hold exactly one molecule");
+        const std::vector<int> shell_atom = hfg::shell_atoms(e, natom, xyz);
+        const size_t N2 = static_cast<size_t>(e->mols[0].nao) * e->mols[0].nao;
+        hfg::DevBuf<double> d;
+        d.alloc(2 * N2 + 3 * static_cast<size_t>(natom));
+        HFG_CUDA(cudaMemcpyAsync(d.p, D, sizeof(double) * N2, cudaMemcpyHostToDevice, e->stream));
+        HFG_CUDA(cudaMemcpyAsync(d.p + N2, W, sizeof(double) * N2, cudaMemcpyHostToDevice, e->stream));
+        HFG_CUDA(cudaMemsetAsync(d.p + 2 * N2, 0, sizeof(double) * 3 * natom, e->stream));
+        hfg::gradient_one_electron_device(e, shell_atom, natom, Z, xyz, d.p, d.p + N2, d.p + 2 * N2);
+        std::vector<double> g1(static_cast<size_t>(3) * natom);
+        HFG_CUDA(cudaMemcpyAsync(g1.data(), d.p + 2 * N2, sizeof(double) * g1.size(), cudaMemcpyDeviceToHost, e->stream));
+        HFG_CUDA(cudaStreamSynchronize(e->stream));
+        for (size_t k = 0; k < g1.size(); ++k) grad[k] += g1[k];
     });
 }
 

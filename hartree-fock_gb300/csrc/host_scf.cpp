@@ -40,6 +40,7 @@ int engine_enqueue_fock(hfg_engine* e, const hfg_fock_request& r);
 void engine_prepare_capture(hfg_engine* e);
 void engine_check_counts(hfg_engine* e, bool mixed);
 int engine_guarded(hfg_engine* e, const std::function<void()>& f);
+void one_electron_device(hfg_engine* e, int natom, const int* Z, const double* xyz, double* S, double* T, double* V);
 
 namespace
 {
@@ -130,14 +131,11 @@ class Scf
         work_.alloc(static_cast<size_t>(lw));
         lwork_ = lw;
 
-        // One-electron part (host FP64), X = S^{-1/2}.
-        std::vector<double> S(N2), T(N2), V(N2), h(N2);
-        const int rc = hfg_one_electron(b, natom, Z, xyz, S.data(), T.data(), V.data());
+        // One-electron part on the device (FP64): S, and h = T + V; X = S^{-1/2}.
+        const int rc = engine_guarded(e, [&] { one_electron_device(e, natom, Z, xyz, S_.p, T1_.p, T2_.p); });
         if (rc != HFG_OK)
-            throw ScfError(rc, "scf: one-electron integrals failed");
-        for (size_t k = 0; k < N2; ++k) h[k] = T[k] + V[k];
-        up(S_, S);
-        up(h_, h);
+            throw ScfError(rc, std::string("scf: one-electron integrals failed: ") + hfg_last_error(e));
+        add(h_, 1.0, T1_, 1.0, T2_);
         inverse_sqrt();
     }
 
@@ -646,9 +644,9 @@ class Scf
     void* cublas_ws_     = nullptr;
     DiisDevice dd_dev_ {};
     MeasureDevice md_ {};
-    cudaGraph_t graph_         = nullptr;
-    cudaGraphExec_t graph_exec_ = nullptr;
-    bool graph_failed_          = false;
+    cudaGraph_t seg_graph_[3] {};
+    cudaGraphExec_t seg_exec_[3] {};
+    bool graph_failed_ = false;
     int replays_                = 0;
     cudaEvent_t gev_[2] {};
 
@@ -719,10 +717,13 @@ class Scf
 
     void free_device_iterations()
     {
-        if (graph_exec_)
-            cudaGraphExecDestroy(graph_exec_);
-        if (graph_)
-            cudaGraphDestroy(graph_);
+        for (int k = 0; k < 3; ++k)
+        {
+            if (seg_exec_[k])
+                cudaGraphExecDestroy(seg_exec_[k]);
+            if (seg_graph_[k])
+                cudaGraphDestroy(seg_graph_[k]);
+        }
         for (auto& ev : gev_)
             if (ev)
                 cudaEventDestroy(ev);
@@ -738,97 +739,127 @@ class Scf
             cudaFree(cublas_ws_);
     }
 
-    // One iteration's work on the stream, no host synchronisation when `capture`: dD, the Fock build,
-    // F = F_prev + J - K, DIIS (device), the orbital step without damping or level shift, the measures and
-    // their copy to pinned memory.
-    void enqueue_iteration(bool capture)
+    // One iteration is enqueued as segments separated by the eigensolver calls, because cuSOLVER's syevd
+    // refuses stream capture (and a refused capture leaves its handle unusable, so it is never attempted):
+    //   segment 0   dD, the Fock build, F = F_prev + J - K, DIIS (device), F'_alpha = X^T F_alpha X
+    //   syevd(F'_alpha)                                                                   (eager)
+    //   segment 1   C_alpha, D_alpha; RHF: the beta copies, D_tot, the measures; UHF: F'_beta = X^T F_beta X
+    //   UHF: syevd(F'_beta), segment 2   C_beta, D_beta, D_tot, the measures
+    // No segment synchronises with the host, so from the second iteration on each one is captured once and
+    // replayed (`capture`: enqueue into the capture that is open on the stream).
+    void segment(int k, bool capture)
     {
         const long long N2 = static_cast<long long>(n_) * n_;
-        add(dDt_, 1.0, Dt_, -1.0, Dtp_);
-        add(dDa_, 1.0, Da_, -1.0, Dap_);
-        if (uhf_)
-            add(dDb_, 1.0, Db_, -1.0, Dbp_);
-        hfg_fock_request r {};
-        r.unrestricted       = uhf_ ? 1 : 0;
-        r.precision          = o_.precision;
-        r.device_pointers    = 1;
-        r.schwartz_threshold = o_.schwartz_threshold;
-        r.density_threshold  = o_.density_threshold;
-        r.fp32_cutoff        = o_.fp32_cutoff;
-        r.dD_tot             = dDt_.p;
-        r.dD_alpha           = dDa_.p;
-        r.dD_beta            = uhf_ ? dDb_.p : nullptr;
-        r.J                  = J_.p;
-        r.K_alpha            = Ka_.p;
-        r.K_beta             = uhf_ ? Kb_.p : nullptr;
-        if (capture)
+        if (k == 0)
         {
-            ck(cudaEventRecord(gev_[0], s_), "event");
-            const int rc = engine_guarded(eng_, [&] { engine_enqueue_fock(eng_, r); });
-            if (rc != HFG_OK)
-                throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
-            ck(cudaEventRecord(gev_[1], s_), "event");
-        }
-        else
-        {
-            hfg_fock_stats st {};
-            const int rc = hfg_fock_direct(eng_, &r, &st);
-            if (rc != HFG_OK)
-                throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
-            ms_fock_ += st.ms_total;
-        }
-        add(Fa_, 1.0, Fap_, 1.0, J_);
-        add(Fa_, 1.0, Fa_, -1.0, Ka_);
-        copy(Fap_, Fa_);
-        if (uhf_)
-        {
-            add(Fb_, 1.0, Fbp_, 1.0, J_);
-            add(Fb_, 1.0, Fb_, -1.0, Kb_);
-            copy(Fbp_, Fb_);
-        }
-        else
-        {
-            copy(Fb_, Fa_);
-            copy(Fbp_, Fap_);
-        }
-        if (o_.use_diis)
-        {
-            // e = (F_a D_a S - S D_a F_a) + (beta) into e_, as diis_update does.
-            const double one = 1.0, mone = -1.0;
-            auto comm = [&](const DMat& F, const DMat& D, bool accumulate) {
-                gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, F.p, D.p, 0.0, T1_.p);
-                gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, T1_.p, S_.p, 0.0, T2_.p);
-                ck(cublasDgeam(cb_, CUBLAS_OP_N, CUBLAS_OP_T, n_, n_, &one, T2_.p, n_, &mone, T2_.p, n_, T1_.p, n_), "geam");
-                if (accumulate)
-                    add(e_, 1.0, e_, 1.0, T1_);
-                else
-                    copy(e_, T1_);
-            };
-            comm(Fa_, Da_, false);
-            comm(Fb_, Db_, true);
-            ck(hfg::diis_push(dd_dev_, Fa_.p, Fb_.p, e_.p, N2, s_), "diis_push");
-            ck(hfg::diis_extrapolate(dd_dev_, Fa_.p, Fb_.p, dsc_, N2, s_), "diis_extrapolate");
+            add(dDt_, 1.0, Dt_, -1.0, Dtp_);
+            add(dDa_, 1.0, Da_, -1.0, Dap_);
+            if (uhf_)
+                add(dDb_, 1.0, Db_, -1.0, Dbp_);
+            hfg_fock_request r {};
+            r.unrestricted       = uhf_ ? 1 : 0;
+            r.precision          = o_.precision;
+            r.device_pointers    = 1;
+            r.schwartz_threshold = o_.schwartz_threshold;
+            r.density_threshold  = o_.density_threshold;
+            r.fp32_cutoff        = o_.fp32_cutoff;
+            r.dD_tot             = dDt_.p;
+            r.dD_alpha           = dDa_.p;
+            r.dD_beta            = uhf_ ? dDb_.p : nullptr;
+            r.J                  = J_.p;
+            r.K_alpha            = Ka_.p;
+            r.K_beta             = uhf_ ? Kb_.p : nullptr;
+            if (capture)
+            {
+                ck(cudaEventRecord(gev_[0], s_), "event");
+                const int rc = engine_guarded(eng_, [&] { engine_enqueue_fock(eng_, r); });
+                if (rc != HFG_OK)
+                    throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
+                ck(cudaEventRecord(gev_[1], s_), "event");
+            }
+            else
+            {
+                hfg_fock_stats st {};
+                const int rc = hfg_fock_direct(eng_, &r, &st);
+                if (rc != HFG_OK)
+                    throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
+                ms_fock_ += st.ms_total;
+            }
+            add(Fa_, 1.0, Fap_, 1.0, J_);
+            add(Fa_, 1.0, Fa_, -1.0, Ka_);
+            copy(Fap_, Fa_);
+            if (uhf_)
+            {
+                add(Fb_, 1.0, Fbp_, 1.0, J_);
+                add(Fb_, 1.0, Fb_, -1.0, Kb_);
+                copy(Fbp_, Fb_);
+            }
+            else
+            {
+                copy(Fb_, Fa_);
+                copy(Fbp_, Fap_);
+            }
+            if (o_.use_diis)
+            {
+                // e = (F_a D_a S - S D_a F_a) + (beta) into e_, as diis_update does.
+                const double one = 1.0, mone = -1.0;
+                auto comm = [&](const DMat& F, const DMat& D, bool accumulate) {
+                    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, F.p, D.p, 0.0, T1_.p);
+                    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, T1_.p, S_.p, 0.0, T2_.p);
+                    ck(cublasDgeam(cb_, CUBLAS_OP_N, CUBLAS_OP_T, n_, n_, &one, T2_.p, n_, &mone, T2_.p, n_, T1_.p, n_),
+                       "geam");
+                    if (accumulate)
+                        add(e_, 1.0, e_, 1.0, T1_);
+                    else
+                        copy(e_, T1_);
+                };
+                comm(Fa_, Da_, false);
+                comm(Fb_, Db_, true);
+                ck(hfg::diis_push(dd_dev_, Fa_.p, Fb_.p, e_.p, N2, s_), "diis_push");
+                ck(hfg::diis_extrapolate(dd_dev_, Fa_.p, Fb_.p, dsc_, N2, s_), "diis_extrapolate");
+            }
+            orth(Fa_); // F'_alpha into T1
+            return;
         }
         // Orbital step (SCF.cpp:747-835 without damping and level shifting).
-        eig_orth_nosync(Fa_, Ca_, wa_);
-        copy(Dap_, Da_);
-        density(Ca_, nocc_a_, Da_, 0.0);
-        copy(Dbp_, Db_);
-        if (uhf_)
+        const bool alpha = k == 1;
+        DMat& C = alpha ? Ca_ : Cb_;
+        gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, X_.p, T1_.p, 0.0, C.p);
+        if (alpha)
         {
-            eig_orth_nosync(Fb_, Cb_, wb_);
-            density(Cb_, nocc_b_, Db_, 0.0);
-        }
-        else
-        {
+            copy(Dap_, Da_);
+            density(Ca_, nocc_a_, Da_, 0.0);
+            copy(Dbp_, Db_);
+            if (uhf_)
+            {
+                orth(Fb_); // F'_beta into T1 for the next eigensolve
+                return;
+            }
             copy(Cb_, Ca_);
             copy_vec(wb_, wa_);
             copy(Db_, Da_);
         }
+        else
+            density(Cb_, nocc_b_, Db_, 0.0);
         copy(Dtp_, Dt_);
         add(Dt_, 1.0, Da_, 1.0, Db_);
         ck(scf_measures(md_, N2, s_), "measures");
         ck(cudaMemcpyAsync(hsc_, dsc_, sizeof(ScfScalars), cudaMemcpyDeviceToHost, s_), "d2h");
+    }
+
+    // T1 = X^T F X.
+    void orth(const DMat& F)
+    {
+        gemm(CUBLAS_OP_T, CUBLAS_OP_N, n_, n_, n_, 1.0, X_.p, F.p, 0.0, T2_.p);
+        gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, T2_.p, X_.p, 0.0, T1_.p);
+    }
+
+    // Eigenvectors of T1 in place, eigenvalues into w (its status is checked after the iterations).
+    void eigensolve(DMat& w)
+    {
+        ck(cusolverDnDsyevd(cs_, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n_, T1_.p, n_, w.p, work_.p, lwork_,
+                            info_),
+           "syevd");
     }
 
     void read_measures()
@@ -841,40 +872,53 @@ class Scf
             diis_err_ = hsc_->diis_error;
     }
 
+    // Captures segment k (nothing of it runs); false if the capture was refused.
+    bool capture_segment(int k)
+    {
+        ck(cudaStreamBeginCapture(s_, cudaStreamCaptureModeRelaxed), "begin capture");
+        bool ok = true;
+        try
+        {
+            segment(k, true);
+        }
+        catch (const ScfError&)
+        {
+            ok = false;
+        }
+        cudaGraph_t g       = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(s_, &g);
+        if (ok && e == cudaSuccess && g && cudaGraphInstantiate(&seg_exec_[k], g, 0) == cudaSuccess)
+        {
+            seg_graph_[k] = g;
+            return true;
+        }
+        if (g)
+            cudaGraphDestroy(g);
+        seg_exec_[k] = nullptr;
+        cudaGetLastError(); // clear the refused capture's error state
+        return false;
+    }
+
     void device_iteration(int it)
     {
         ++builds_;
-        if (it > 0 && !graph_exec_ && !graph_failed_)
+        const int nseg = uhf_ ? 3 : 2;
+        if (it > 0 && !seg_exec_[0] && !graph_failed_)
+            for (int k = 0; k < nseg && !graph_failed_; ++k)
+                graph_failed_ = !capture_segment(k);
+        const bool replay = !graph_failed_ && seg_exec_[0];
+        for (int k = 0; k < nseg; ++k)
         {
-            // Capture this iteration; if the capture is refused (a call inside cannot be captured), run the
-            // rest eagerly.  Nothing of a refused capture has run, so the iteration is then done eagerly.
-            ck(cudaStreamBeginCapture(s_, cudaStreamCaptureModeRelaxed), "begin capture");
-            bool ok = true;
-            try
-            {
-                enqueue_iteration(true);
-            }
-            catch (const ScfError&)
-            {
-                ok = false;
-            }
-            cudaGraph_t g      = nullptr;
-            const cudaError_t e = cudaStreamEndCapture(s_, &g);
-            if (ok && e == cudaSuccess && g && cudaGraphInstantiate(&graph_exec_, g, 0) == cudaSuccess)
-                graph_ = g;
+            if (replay)
+                ck(cudaGraphLaunch(seg_exec_[k], s_), "graph launch");
             else
-            {
-                if (g)
-                    cudaGraphDestroy(g);
-                graph_exec_   = nullptr;
-                graph_failed_ = true;
-                cudaGetLastError(); // clear the refused capture's error state
-            }
+                segment(k, false);
+            if (k + 1 < nseg)
+                eigensolve(k == 0 ? wa_ : wb_);
         }
-        if (graph_exec_)
+        read_measures();
+        if (replay)
         {
-            ck(cudaGraphLaunch(graph_exec_, s_), "graph launch");
-            read_measures();
             const int rc = engine_guarded(eng_, [&] { engine_check_counts(eng_, o_.precision == HFG_PRECISION_MIXED); });
             if (rc != HFG_OK)
                 throw ScfError(rc, std::string("scf: Fock build failed: ") + hfg_last_error(eng_));
@@ -883,22 +927,6 @@ class Scf
                 ms_fock_ += ms;
             ++replays_;
         }
-        else
-        {
-            enqueue_iteration(false);
-            read_measures();
-        }
-    }
-
-    // eig_orth without level shift and without the host read of syevd's status (checked after the loop).
-    void eig_orth_nosync(const DMat& F, DMat& C, DMat& w)
-    {
-        gemm(CUBLAS_OP_T, CUBLAS_OP_N, n_, n_, n_, 1.0, X_.p, F.p, 0.0, T2_.p);
-        gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, T2_.p, X_.p, 0.0, T1_.p);
-        ck(cusolverDnDsyevd(cs_, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n_, T1_.p, n_, w.p, work_.p, lwork_,
-                            info_),
-           "syevd");
-        gemm(CUBLAS_OP_N, CUBLAS_OP_N, n_, n_, n_, 1.0, X_.p, T1_.p, 0.0, C.p);
     }
 
     // <S^2> = Sz(Sz+1) + N_beta - |C_a,occ^T S C_b,occ|^2 (SCF.cpp:838-845).

@@ -126,6 +126,10 @@ def lib():
         L.hfg_gradient.argtypes = [vp, ctypes.POINTER(GradRequest), dpp, dpp]
         L.hfg_boys_eval.argtypes = [ip, ip, ip, ctypes.c_longlong, dpp, dpp]
         L.hfg_store_integrals.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ctypes.c_size_t)]
+        L.hfg_one_electron_gpu.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), dpp, dpp, dpp, dpp]
+        L.hfg_gradient_one_electron_gpu.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), dpp, dpp, dpp, dpp]
+        L.hfg_gradient_one_electron.argtypes = [ctypes.POINTER(_Basis), ctypes.POINTER(ctypes.c_int), ip,
+                                                ctypes.POINTER(ctypes.c_int), dpp, dpp, dpp, dpp]
         L.hfg_fock_conventional.argtypes = [vp, ctypes.POINTER(_Request), ctypes.POINTER(Stats)]
         _lib = L
     return _lib
@@ -230,6 +234,26 @@ class Engine:
             n = self.nao
             outs = [o.reshape(n, n, order="F") if o is not None else None for o in outs]
         return outs[0], outs[1], outs[2], st.as_dict()
+
+    def one_electron(self, Z, xyz):
+        """S, T, V of this engine's molecule computed on the GPU (FP64)."""
+        n = self.nao
+        S, T, V = (np.zeros((n, n), order="F") for _ in range(3))
+        Zc = np.ascontiguousarray(Z, dtype=np.int32)
+        X = np.ascontiguousarray(xyz, dtype=np.float64)
+        self._check(lib().hfg_one_electron_gpu(self.h, len(Zc), Zc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(X),
+                                               _dp(S), _dp(T), _dp(V)))
+        return S, T, V
+
+    def gradient_one_electron(self, Z, xyz, D, W):
+        """sum D d(T+V)/dX - W dS/dX on the GPU (natom x 3); D total density, W energy-weighted density."""
+        Zc = np.ascontiguousarray(Z, dtype=np.int32)
+        X = np.ascontiguousarray(xyz, dtype=np.float64)
+        g = np.zeros((len(Zc), 3))
+        Df, Wf = (np.asfortranarray(a, dtype=np.float64) for a in (D, W))
+        self._check(lib().hfg_gradient_one_electron_gpu(self.h, len(Zc), Zc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                        _dp(X), _dp(Df), _dp(Wf), _dp(g)))
+        return g
 
     def store_integrals(self, sthr=1e-10) -> int:
         """Evaluate and keep every Schwartz-surviving integral (the DIRECT FALSE path); returns the bytes."""

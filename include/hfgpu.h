@@ -216,6 +216,11 @@ void* hfg_stream(hfg_engine* engine);
 int hfg_one_electron(const hfg_basis* basis, int natom, const int* Z, const double* xyz, double* S, double* T,
                      double* V);
 
+/* The same S, T, V computed on the GPU of `engine` (its single molecule's basis), FP64, host outputs.  The
+ * SCF driver uses this device path. */
+int hfg_one_electron_gpu(hfg_engine* engine, int natom, const int* Z, const double* xyz, double* S, double* T,
+                         double* V);
+
 /* SCFOptions (include/SCF.hpp:9-32) plus the engine's own knobs. */
 typedef struct hfg_scf_options
 {
@@ -240,10 +245,12 @@ typedef struct hfg_scf_options
     double fp32_cutoff;        /* FP32 cutoff of the mixed mode (1e-4) */
     int full_rebuild_every;    /* 0: incremental builds as the reference; k > 0: full build every k iterations */
     int verbose;               /* print the iteration table to stdout */
-    int graph_iterations;      /* 1: run every SCF iteration after the first as one replayed CUDA graph (Fock build,
-                                  DIIS on the device, orbital step, energy and convergence measures; one host
-                                  read-back per iteration).  Used when damping and level shifting are off and
-                                  DIIS_SIZE <= 16; otherwise, or if the capture is refused, iterations run eagerly. */
+    int graph_iterations;      /* 1: every SCF iteration after the first replays CUDA graphs captured once: the Fock
+                                  build, F update, DIIS on the device, X^T F X, the orbital update, energy and
+                                  convergence measures, in segments around the eigensolver calls (cuSOLVER's syevd,
+                                  which refuses capture, runs between them); one host read-back per iteration.
+                                  Used when damping and level shifting are off and DIIS_SIZE <= 16; otherwise, or if
+                                  a capture is refused, the same device iterations run eagerly. */
     int direct;                /* DIRECT (1).  0: the stored-integral SCF (SCF.cpp:233-521): integrals stored once by
                                   hfg_store_integrals, every Fock build F = h + J[D] - K[D] from them */
 } hfg_scf_options;
@@ -278,8 +285,8 @@ int hfg_core_guess(hfg_engine* engine, const hfg_scf_options* opt, int natom, co
  * central finite differences of its energy).  The backward half of the forward/backward pair whose
  * forward half is hfg_scf_run: with D_alpha == NULL the densities and energy-weighted density of the
  * last hfg_scf_run on this engine are used.  grad: natom x 3 (Eh/bohr).  Two-electron part on the GPU
- * (FP64 adjoint kernel, E/R tables recomputed), one-electron, overlap and nuclear-repulsion parts FP64 on
- * the host.  The engine must hold one molecule whose shell centres are the nuclei at xyz. */
+ * (adjoint kernel, E/R tables recomputed), one-electron and overlap parts FP64 on the GPU, nuclear
+ * repulsion on the host.  The engine must hold one molecule whose shell centres are the nuclei at xyz. */
 typedef struct hfg_gradient_request
 {
     int natom;
@@ -298,7 +305,14 @@ typedef struct hfg_gradient_request
 
 int hfg_gradient(hfg_engine* engine, const hfg_gradient_request* req, double* grad, double* ms_two_electron);
 
-/* One-electron, overlap (-W dS) and nuclear-repulsion parts of the gradient, added into grad (host). */
+/* One-electron and overlap parts of the gradient (sum D d(T+V)/dX - W dS/dX) on the GPU of `engine`, added
+ * into grad (host, natom x 3); D is the total density, W the total energy-weighted density (host).
+ * hfg_gradient uses this device path together with the nuclear-repulsion term. */
+int hfg_gradient_one_electron_gpu(hfg_engine* engine, int natom, const int* Z, const double* xyz, const double* D,
+                                  const double* W, double* grad);
+
+/* One-electron, overlap (-W dS) and nuclear-repulsion parts of the gradient, added into grad (host CPU code,
+ * FP64, OpenMP). */
 int hfg_gradient_one_electron(const hfg_basis* basis, const int* shell_atom, int natom, const int* Z,
                               const double* xyz, const double* D, const double* W, double* grad);
 

@@ -647,9 +647,11 @@ long orc_fock_direct(const orc_basis* B, const double* Q, const double* dDtot, c
     return survivors;
 }
 
-/* The same build restricted to the canonical quartets whose bra pair (a >= b) is flagged in
- * bra_mask[a*(a+1)/2 + b]: a bounded sample of one build, used to time the CPU baseline on workloads
- * whose full build takes too long on a CPU.  Returns the surviving quartets evaluated. */
+/* The same build restricted to the ordered bra pairs (a, b) flagged in bra_mask[a * ns + b]: a bounded
+ * sample of one build, used to time the CPU baseline on workloads whose full build takes too long on a
+ * CPU.  For each sampled bra the whole ket range (c, d) in [0, ns)^2 is scanned with the skip tests of the
+ * full build's nShells^4 loop (SCF.cpp:592-600), so that a sample of a fraction f of the ordered bra pairs
+ * costs f of the full build, scan included.  Returns the surviving quartets evaluated. */
 long orc_fock_direct_sample(const orc_basis* B, const double* Q, const double* dDtot, const double* dDa,
                             const double* dDb, double sthr, double dthr, const unsigned char* bra_mask, double* J,
                             double* Ka, double* Kb)
@@ -667,7 +669,7 @@ long orc_fock_direct_sample(const orc_basis* B, const double* Q, const double* d
     memset(Ka, 0, sizeof(double) * N * N);
     if (Kb)
         memset(Kb, 0, sizeof(double) * N * N);
-    const long npairs = (long)ns * (ns + 1) / 2;
+    const long npairs = (long)ns * ns;
     long nsel = 0;
     for (long p = 0; p < npairs; ++p) nsel += bra_mask[p] ? 1 : 0;
     long* sel = (long*)malloc(sizeof(long) * (nsel > 0 ? nsel : 1));
@@ -685,15 +687,12 @@ long orc_fock_direct_sample(const orc_basis* B, const double* Q, const double* d
 #pragma omp for schedule(dynamic, 1) nowait
         for (long s = 0; s < nsel; ++s)
         {
-            const long ab = sel[s];
-            long a = 0;
-            while ((a + 1) * (a + 2) / 2 <= ab) ++a;
-            const long b = ab - a * (a + 1) / 2;
-            for (long cd = 0; cd <= ab; ++cd)
+            const long a = sel[s] / ns, b = sel[s] % ns;
+            for (long r = 0; r < (long)ns * ns; ++r)
             {
-                long c = 0;
-                while ((c + 1) * (c + 2) / 2 <= cd) ++c;
-                const long d = cd - c * (c + 1) / 2;
+                const long c = r / ns, d = r % ns;
+                if (b > a || d > c || a * (a + 1) / 2 + b < c * (c + 1) / 2 + d)
+                    continue;
                 if (!quartet_survives(ns, Q, Mt, Ma, Mb, a, b, c, d, sthr, dthr))
                     continue;
                 ++survivors;

@@ -131,7 +131,7 @@ class Basis:
         return J, Ka, Kb, ns
 
     def fock_direct_sample(self, Q, dDtot, dDa, bra_mask, dDb=None, sthr=1e-10, dthr=1e-10):
-        """The build restricted to bra pairs flagged in bra_mask (length nshells*(nshells+1)/2)."""
+        """The build restricted to the ordered bra pairs (a, b) flagged in bra_mask[a * nshells + b]."""
         N = self.nao
         J, Ka = np.zeros((N, N), order="F"), np.zeros((N, N), order="F")
         Kb = np.zeros((N, N), order="F") if dDb is not None else None

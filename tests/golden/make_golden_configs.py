@@ -79,7 +79,11 @@ def make_fd_w8():
     Z, xyz0 = w.water_lattice(2, 2, 2)
     path = os.path.join(HERE, "cfg_fd_w8_ccpvdz.npz")
     g = np.full(len(FD_COORDS), np.nan)
+    if os.path.exists(path):  # resume: keep the coordinates already done
+        g = np.array(np.load(path)["grad_fd"], dtype=float)
     for k, (a, ax) in enumerate(FD_COORDS):
+        if not np.isnan(g[k]):
+            continue
         xp, xm = xyz0.copy(), xyz0.copy()
         xp[a, ax] += FD_STEP
         xm[a, ax] -= FD_STEP
