@@ -506,7 +506,8 @@ def batch_timings(dev, cutoff, steps, warmup):
     ptrs = dict(dD_tot=d_dt.data_ptr(), dD_alpha=d_da.data_ptr(), J=d_J.data_ptr(), K_alpha=d_K.data_ptr())
     stream = torch.cuda.ExternalStream(eb.stream())
 
-    def timed(prec, graph):
+    def timed(prec, graph, persistent=False):
+        eb.set_persistent(persistent)
         eb.set_graph_mode(graph)
         for _ in range(max(warmup, 3)):
             eb.fock_device(ptrs, precision=prec, fp32_cutoff=cutoff)
@@ -536,14 +537,23 @@ def batch_timings(dev, cutoff, steps, warmup):
     ms_mixed, st_mixed = timed(MIXED, False)
     ms_graph, _ = timed(MIXED, True)
     e32 = e2_per_molecule()
+    ms_pers, st_pers = timed(MIXED, False, persistent=True)
+    e32p = e2_per_molecule()
+    ms_pers_graph, _ = timed(MIXED, True, persistent=True)
     eb.set_graph_mode(False)
+    eb.set_persistent(False)
     nmol = len(mols)
     return {"molecules": nmol, "basis": "6-31G", "nao_total": int(sum(D.shape[0] for D in dens)),
             "k_range": [1, 12], "seed": 0,
             "fock_builds_per_s": {"fp64": nmol / (ms64 * 1e-3), "mixed": nmol / (ms_mixed * 1e-3),
-                                  "mixed_graph": nmol / (ms_graph * 1e-3)},
-            "ms_per_batched_build": {"fp64": ms64, "mixed": ms_mixed, "mixed_graph": ms_graph},
-            "kernel_launches_per_build": {"eager": st_mixed["kernel_launches"], "graph": "1 graph launch"},
+                                  "mixed_graph": nmol / (ms_graph * 1e-3),
+                                  "mixed_persistent": nmol / (ms_pers * 1e-3),
+                                  "mixed_persistent_graph": nmol / (ms_pers_graph * 1e-3)},
+            "ms_per_batched_build": {"fp64": ms64, "mixed": ms_mixed, "mixed_graph": ms_graph,
+                                     "mixed_persistent": ms_pers, "mixed_persistent_graph": ms_pers_graph},
+            "kernel_launches_per_build": {"eager": st_mixed["kernel_launches"],
+                                          "persistent": st_pers["kernel_launches"], "graph": "1 graph launch"},
+            "max_abs_delta_e2_persistent_vs_per_class": float(np.max(np.abs(e32p - e32))),
             "max_abs_delta_e2_per_molecule": float(np.max(np.abs(e32 - e64))),
             "quartets": {"fp64": int(sum(st_mixed["quartets_fp64"])), "fp32": int(sum(st_mixed["quartets_fp32"]))}}
 

@@ -52,6 +52,12 @@ constexpr int chunk_width(bool fp32)
         return 0;
     return (QC == 12 || QC == 13) ? 3 : QC == 14 ? 2 : (QC >= 16 && QC <= 19) ? 1 : 0;
 }
+// The form a launch with form 0 runs (before or without autotuning): the chunked form where it measured
+// fastest at full size ((H2O)_64/6-31G**: (dp|dp), (dd|pp), (dd|ds), (dd|dp) in FP32), else warp or thread.
+constexpr int default_form(bool fp32)
+{
+    return (fp32 && (QC == 14 || (QC >= 17 && QC <= 19))) ? kFormChunk : (warp_form(fp32) ? kFormWarp : kFormThread);
+}
 constexpr unsigned form_mask(bool fp32)
 {
     return (warp_form(fp32) || dual_form(fp32) ? (1u << kFormWarp) : 0u) |
@@ -71,7 +77,7 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
     constexpr bool kWarpForm = warp_form(sizeof(Real) == 4);
     if (c.count_host == 0)
         return cudaSuccess;
-    const int form = c.form == 0 ? (kWarpForm ? kFormWarp : kFormThread) : c.form;
+    const int form = c.form == 0 ? default_form(sizeof(Real) == 4) : c.form;
     if (!((form_mask(sizeof(Real) == 4) >> form) & 1u))
         return cudaErrorInvalidValue;
     const size_t slice_bytes = sizeof(Real) * BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow;
@@ -199,7 +205,7 @@ cudaError_t HFG_CAT(launch_stored_, HFG_QCLASS)(const StoredLaunch& c)
 
 unsigned HFG_CAT(class_form_mask_, HFG_QCLASS)(bool fp32)
 {
-    return form_mask(fp32) | (static_cast<unsigned>(warp_form(fp32) ? kFormWarp : kFormThread) << 16);
+    return form_mask(fp32) | (static_cast<unsigned>(default_form(fp32)) << 16);
 }
 #elif HFG_PART == 1
 cudaError_t HFG_CAT(launch_class32_, HFG_QCLASS)(const ClassLaunch& c)

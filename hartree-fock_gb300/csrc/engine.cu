@@ -23,6 +23,7 @@
 #include "eri_grad.cuh"
 #include "hfgpu.h"
 #include "onee.h"
+#include "persistent.h"
 
 #include <algorithm>
 #include <array>
@@ -244,6 +245,9 @@ struct hfg_engine
     // CUDA-graph replay of whole builds (hfg_set_graph_mode): the graph of the last device-pointer
     // request, valid while the request key matches and no buffer it uses has been reallocated.
     bool graph_mode = false;
+    // Persistent work-queue launch of the small classes (hfg_set_persistent) and its item counter.
+    bool persistent = false;
+    hfg::DevBuf<unsigned long long> d_pcounter;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     struct GraphKey
@@ -1353,15 +1357,65 @@ static int enqueue_build(hfg_engine* e, const hfg_fock_request& r, bool graph, i
         HFG_CUDA(cudaEventRecord(e->ev2[0], s));
         HFG_CUDA(cudaStreamWaitEvent(e->stream2, e->ev2[0], 0));
     }
+    auto make_view = [&](int prec) {
+        FockView v  = base_view(e, prec == 1);
+        v.pairs     = e->d_spairs.p;
+        v.Dt        = prec == 1 ? static_cast<const void*>(e->d_dDf[0].p) : e->d_dD[0].p;
+        v.Da        = prec == 1 ? static_cast<const void*>(e->d_dDf[1].p) : e->d_dD[1].p;
+        v.Db        = prec == 1 ? static_cast<const void*>(e->d_dDf[2].p) : e->d_dD[2].p;
+        v.X         = e->d_acc[0].p;
+        v.Ya        = e->d_acc[1].p;
+        v.Yb        = e->d_acc[2].p;
+        v.ao_thr    = r.schwartz_threshold;
+        v.ao_thr_f  = static_cast<float>(r.schwartz_threshold);
+        return v;
+    };
+    // Persistent mode: one work-queue launch for the small classes of both precisions on `s` (it runs
+    // beside the FP32 classes on stream2); those classes are skipped below.
+    const bool persist = e->persistent;
+    auto in_queue = [&](int qc) {
+        return persist && (qc == kPersistentClasses[0] || qc == kPersistentClasses[1] || qc == kPersistentClasses[2] ||
+                           qc == kPersistentClasses[3]);
+    };
+    if (persist)
+    {
+        if (!graph)
+            HFG_CUDA(cudaEventRecord(e->ev[3], s));
+        PersistentArgs pa {};
+        bool any = false;
+        for (int seg = 0; seg < kPersistentSegments; ++seg)
+        {
+            const int prec = seg / 4, qc = kPersistentClasses[seg % 4];
+            if ((prec == 1 && !mixed) || e->cap[qc] == 0 || (!graph && e->h_counts[2 * qc + prec] == 0))
+                continue;
+            const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
+            const int P2 = qc - P1 * (P1 + 1) / 2;
+            const int L  = pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2);
+            pa.list[seg]  = e->d_list[qc][prec].p;
+            pa.count[seg] = e->d_counts.p + 2 * qc + prec;
+            pa.slice[seg] = prec == 1 ? static_cast<const void*>(e->d_boys32[L].p) : e->d_boys64[L].p;
+            form_ran[qc][prec] = kFormPersistent;
+            any = true;
+        }
+        if (any)
+        {
+            pa.view[0] = make_view(0);
+            pa.view[1] = make_view(mixed ? 1 : 0);
+            e->d_pcounter.alloc(1);
+            pa.counter = e->d_pcounter.p;
+            HFG_CUDA(launch_persistent(pa, uhf, s, e->num_sms));
+            ++launches;
+        }
+    }
     for (int prec = 0; prec < (mixed ? 2 : 1); ++prec)
     {
         cudaStream_t ps = (overlap && prec == 1) ? e->stream2 : s;
-        if (!graph)
+        if (!graph && !(persist && prec == 0))
             HFG_CUDA(cudaEventRecord(overlap && prec == 1 ? e->ev2[2] : e->ev[3 + prec], ps));
         for (int qc = kNumQuartetClasses - 1; qc >= 0; --qc)
         {
             const unsigned long long n = graph ? e->cap[qc] : e->h_counts[2 * qc + prec];
-            if (n == 0)
+            if (n == 0 || in_queue(qc))
                 continue;
             const int P1 = [&] { int p = 0; while ((p + 1) * (p + 2) / 2 <= qc) ++p; return p; }();
             const int P2 = qc - P1 * (P1 + 1) / 2;
@@ -2431,6 +2485,15 @@ int hfg_set_precision_shares(hfg_engine* e, double share_fp64, double share_fp32
     hfg::invalidate_graph(e);
     e->overlap_share   = static_cast<float>(share_fp64);
     e->overlap_share32 = static_cast<float>(share_fp32);
+    return HFG_OK;
+}
+
+int hfg_set_persistent(hfg_engine* e, int on)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    hfg::invalidate_graph(e);
+    e->persistent = on != 0;
     return HFG_OK;
 }
 

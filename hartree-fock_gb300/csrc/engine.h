@@ -29,6 +29,7 @@ struct ClassLaunch
 };
 // Kernel forms of a class kernel (eri_jk.cuh, eri_warp.cuh, eri_group.cuh).
 constexpr int kFormThread = 1, kFormWarp = 2, kFormGroup = 3, kFormChunk = 4;
+constexpr int kFormPersistent = 5; // reported in the stats only: the class ran in the persistent work queue
 using ClassLauncher = cudaError_t (*)(const ClassLaunch&);
 // Defined in classes.cu (one translation unit per quartet class).
 cudaError_t launch_class(int qclass, const ClassLaunch& L);

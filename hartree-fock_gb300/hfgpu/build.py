@@ -60,7 +60,7 @@ def _units():
         for part in range(3):  # FP64 Fock kernels, FP32 Fock kernels, gradient kernels
             flags = NVCC_FLAGS + [f"-DHFG_QCLASS={c}", f"-DHFG_PART={part}"]
             units.append(("nvcc", src, flags, f"class{c:02d}p{part}", hdrs))
-    for name in ("engine.cu", "dispatch.cu", "peak.cu", "boys_check.cu", "scf_device.cu", "onee.cu"):
+    for name in ("engine.cu", "dispatch.cu", "peak.cu", "boys_check.cu", "scf_device.cu", "onee.cu", "persistent.cu"):
         units.append(("nvcc", os.path.join(CSRC, name), NVCC_FLAGS, name[:-3], hdrs))
     for name in sorted(os.listdir(CSRC)):
         if name.endswith(".cpp"):

@@ -154,6 +154,7 @@ int hfg_fock_conventional(hfg_engine* engine, const hfg_fock_request* req, hfg_f
 #define HFG_FORM_WARP 2
 #define HFG_FORM_GROUP 3
 #define HFG_FORM_CHUNK 4 /* one thread per (quartet, chunk of ket Cartesian components): the FP32 d classes */
+#define HFG_FORM_PERSISTENT 5 /* in hfg_fock_stats only: the class ran in the persistent work queue */
 /* Set the form of class `qclass` (-1: every class) at precision `fp32` (0: FP64 kernels, 1: FP32
  * kernels).  HFG_FORM_AUTO forgets earlier timings; a form the class was not compiled in returns
  * HFG_ERR_UNSUPPORTED (with qclass -1 such classes keep AUTO). */
@@ -177,6 +178,13 @@ int hfg_set_precision_shares(hfg_engine* engine, double share_fp64, double share
  * always run eagerly. */
 int hfg_set_graph_mode(hfg_engine* engine, int on);
 
+/* Persistent work-queue launch (no reference counterpart; the reference's loop is SCF.cpp:592-728): when on,
+ * the quartet lists of (ss|ss), (ps|ss), (ps|ps) and (pp|ss), FP64 and FP32, are worked through by ONE
+ * launch whose blocks take 128-quartet items from a shared counter (no block waits on another); the other
+ * classes keep their own launches.  Off by default.  Builds with it on or off give the same matrices to
+ * rounding (the digestion's atomics sum in a different order). */
+int hfg_set_persistent(hfg_engine* engine, int on);
+
 /* Forms in use: forms[qc] for the given precision and spin case, 0 where AUTO has not decided yet.
  * `available` (may be NULL) receives the bit mask of compiled forms per class (bit f = form f). */
 int hfg_kernel_forms(hfg_engine* engine, int fp32, int unrestricted, int forms[HFG_NUM_CLASSES],
@@ -199,8 +207,9 @@ int hfg_eri_block(hfg_engine* engine, int a, int b, int c, int d, double* out);
  * device array per GPU (held until the process exits), so one block may hold at most 2016 values
  * (every s/p/d block fits; larger requests fail with HFG_ERR_INVALID).  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that device current: make that first
- * call before any stream capture.  Calls on one device share the array: calls that overlap on the GPU
- * (from several host threads or engines at once) race. */
+ * call before any stream capture.  The address is kept per device for the life of the process: after a
+ * cudaDeviceReset the library must be reloaded before this entry point is used again.  Calls on one device
+ * share the array: calls that overlap on the GPU (from several host threads or engines at once) race. */
 int hfg_eri_block_noalloc(hfg_engine* engine, int a, int b, int c, int d, double* out);
 
 /* The CUDA stream the engine launches on (a cudaStream_t), for callers that time or order work. */

@@ -684,13 +684,15 @@ long orc_fock_direct_sample(const orc_basis* B, const double* Q, const double* d
         double* Kap = (double*)calloc(N * N, sizeof(double));
         double* Kbp = Kb ? (double*)calloc(N * N, sizeof(double)) : NULL;
         double G[ORC_MAX_NAO * ORC_MAX_NAO * ORC_MAX_NAO * ORC_MAX_NAO];
-#pragma omp for schedule(dynamic, 1) nowait
-        for (long s = 0; s < nsel; ++s)
+        /* The sampled bras' slices of the full build's flat index q = ((a ns + b) ns + c) ns + d, walked with
+         * the same schedule and decoding as orc_fock_direct. */
+        const long ns2 = (long)ns * ns, ns3 = ns2 * ns;
+#pragma omp for schedule(dynamic, 32) nowait
+        for (long t = 0; t < nsel * ns2; ++t)
         {
-            const long a = sel[s] / ns, b = sel[s] % ns;
-            for (long r = 0; r < (long)ns * ns; ++r)
+            const long q = sel[t / ns2] * ns2 + t % ns2;
+            const long a = q / ns3, b = (q / ns2) % ns, c = (q / ns) % ns, d = q % ns;
             {
-                const long c = r / ns, d = r % ns;
                 if (b > a || d > c || a * (a + 1) / 2 + b < c * (c + 1) / 2 + d)
                     continue;
                 if (!quartet_survives(ns, Q, Mt, Ma, Mb, a, b, c, d, sthr, dthr))

