@@ -46,6 +46,7 @@ for _p in (REPO, os.path.join(REPO, "hartree-fock_gb300")):
 METRIC = "Fock builds/s & SCF time, (H2O)_64/6-31G**: mixed vs FP64 GPU, |ΔE|≤1e-6 Eh"
 WORKLOADS = {
     "h2o64": dict(lattice=(4, 4, 4), basis="6-31G**", name="(H2O)_64 RHF/6-31G** direct Fock build (1600 bf)"),
+    "h2o32": dict(lattice=(4, 4, 2), basis="6-31G**", name="(H2O)_32 RHF/6-31G** direct Fock build (800 bf)"),
     "h2o16": dict(lattice=(4, 2, 2), basis="6-31G**", name="(H2O)_16 RHF/6-31G** direct Fock build (400 bf)"),
 }
 

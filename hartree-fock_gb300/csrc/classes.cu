@@ -215,8 +215,37 @@ cudaError_t HFG_CAT(launch_class32_, HFG_QCLASS)(const ClassLaunch& c)
 #else
 namespace
 {
+// Thread-per-quartet gradient form where the per-thread arrays fit in registers (GradThread::kValues: at
+// most 72 doubles or 160 floats):
+//   FP64: (ss|ss) (ps|ss) (ps|ps) (pp|ss) (ds|ss);  FP32: also (pp|ps) (ds|ps) (dp|ss).
+template <typename Real> constexpr bool grad_thread_form()
+{
+    return GradThread<LA, LB, LC, LD>::kValues <= (sizeof(Real) == 8 ? 72 : 160);
+}
+
+template <typename Real> cudaError_t launch_grad_thread(const GradLaunch& c)
+{
+    const size_t smem = sizeof(Real) * BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow;
+    auto kern         = grad_thread_kernel<LA, LB, LC, LD, Real>;
+    cudaError_t e     = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+    if (e != cudaSuccess)
+        return e;
+    const unsigned long long need = (c.count + 127) / 128;
+    const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * (per_sm > 0 ? per_sm : 1);
+    kern<<<static_cast<unsigned>(need < cap ? need : cap), 128, smem, c.stream>>>(c.list, c.count, c.view,
+                                                                                static_cast<const Real*>(c.boys_slice));
+    return cudaGetLastError();
+}
+
 template <typename Real> cudaError_t launch_grad_t(const GradLaunch& c)
 {
+    if constexpr (grad_thread_form<Real>())
+        if (!c.group_form)
+            return launch_grad_thread<Real>(c);
     using W           = GradLayout<LA, LB, LC, LD>;
     const size_t smem = sizeof(Real) * (BoysGrid<Real>::kPoints * BoysGrid<Real>::kRow + W::kPerWarp * kGradWarps);
     auto kern         = grad_class_kernel<LA, LB, LC, LD, Real>;

@@ -222,7 +222,6 @@ struct hfg_engine
     hfg::DevBuf<double> d_acc[3];  // X, Ya, Yb
     hfg::DevBuf<double> d_out[3];  // J, Ka, Kb
     hfg::DevBuf<double> d_smax[3]; // shell-pair maxima of |dD|
-    hfg::DevBuf<float> d_smaxf[3]; // FP32 copies (precision split only)
     hfg::DevBuf<double> d_smax2;   // 2 * shell maxima of |dD_tot|
     hfg::DevBuf<double> d_store;
     hfg::DevBuf<hfg::Quartet> d_tmp_list;
@@ -248,6 +247,8 @@ struct hfg_engine
     // Persistent work-queue launch of the small classes (hfg_set_persistent) and its item counter.
     bool persistent = false;
     hfg::DevBuf<unsigned long long> d_pcounter;
+    // Gradient kernels: the lane-group form for every class (hfg_set_gradient_form).
+    bool grad_group_only = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     struct GraphKey
@@ -297,12 +298,11 @@ __global__ void sample_list_kernel(const Quartet* __restrict__ list, unsigned lo
 
 // Shell-pair maxima of |dD| (SCF.cpp:544-575) for every molecule block, with exact integer operations
 // on the bit patterns (|x| clears the sign bit; non-negative doubles order like their bits).  M2, when
-// given, receives 2*M (exact), M32 an FP32 copy.
+// given, receives 2*M (exact).
 __global__ void shell_max_kernel(const double* __restrict__ dD, const PairRec* __restrict__ pairs, int npairs,
                                  const long long* __restrict__ mat_off, const int* __restrict__ mat_ld,
                                  const long long* __restrict__ smax_off, const int* __restrict__ nsh,
-                                 const int* __restrict__ sh_nao, double* __restrict__ M, double* __restrict__ M2,
-                                 float* __restrict__ M32)
+                                 const int* __restrict__ sh_nao, double* __restrict__ M, double* __restrict__ M2)
 {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npairs; k += gridDim.x * blockDim.x)
     {
@@ -325,12 +325,19 @@ __global__ void shell_max_kernel(const double* __restrict__ dD, const PairRec* _
             M2[e1] = v2;
             M2[e2] = v2;
         }
-        if (M32)
-        {
-            M32[e1] = static_cast<float>(v);
-            M32[e2] = static_cast<float>(v);
-        }
     }
+}
+
+// The non-negative finite double with bit pattern b as a float, by integer operations (truncating; below
+// FP32's normal range 0, above it +inf).  Monotone in b, so it narrows a maximum taken on the bit patterns.
+__device__ __forceinline__ float narrow_nonneg(long long b)
+{
+    const int e = static_cast<int>(b >> 52); // biased exponent (the sign bit is clear)
+    if (e < 897)
+        return 0.0f;
+    if (e > 1150)
+        return __int_as_float(0x7f800000);
+    return __int_as_float(((e - 896) << 23) | static_cast<int>((b >> 29) & 0x7fffff));
 }
 
 struct BuildArgs
@@ -351,9 +358,6 @@ struct BuildArgs
     const double* Mb; // null for RHF
     const float* Qf1;
     const float* Qf2;
-    const float* Mtf;
-    const float* Maf;
-    const float* Mbf;
     const long long* smax_off;
     const int* nsh;
     double sthr, dthr;
@@ -398,7 +402,6 @@ __global__ void build_lists_kernel(BuildArgs a)
     const long long dthr = __double_as_longlong(a.dthr);
     const long long ra = so + (long long)sa * ns, rb2 = so + (long long)sb * ns;
     const float Qfi = a.Qf1[i];
-    const float dabf = a.mixed ? 2.0f * a.Mtf[so + sa + (long long)sb * ns] : 0.0f; // FP32 copies exist in mixed mode only
     unsigned c64 = 0, c32 = 0;
     unsigned long long p64 = 0, p32 = 0;
     const unsigned long long o64 = a.pass ? a.bra_off[2 * i] : 0ull;
@@ -435,15 +438,8 @@ __global__ void build_lists_kernel(BuildArgs a)
                 if (md >= dthr)
                 {
                     bool lowp = false;
-                    if (a.mixed)
-                    {
-                        // The FP32/FP64 split is this engine's own heuristic: evaluate it in FP32.
-                        float mf = fmaxf(dabf, 2.0f * a.Mtf[so + sc + (long long)sd * ns]);
-                        mf = fmaxf(mf, fmaxf(fmaxf(a.Maf[ra + sc], a.Maf[ra + sd]), fmaxf(a.Maf[rb2 + sc], a.Maf[rb2 + sd])));
-                        if (a.Mbf)
-                            mf = fmaxf(mf, fmaxf(fmaxf(a.Mbf[ra + sc], a.Mbf[ra + sd]), fmaxf(a.Mbf[rb2 + sc], a.Mbf[rb2 + sd])));
-                        lowp = Qfi * a.Qf2[j] * mf < a.cutoff;
-                    }
+                    if (a.mixed) // the FP32/FP64 split is this engine's own heuristic: evaluated in FP32
+                        lowp = Qfi * a.Qf2[j] * narrow_nonneg(md) < a.cutoff;
                     s32 = lowp;
                     s64 = !lowp;
                 }
@@ -1149,15 +1145,14 @@ static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double 
 {
     cudaStream_t s  = e->stream;
     const int nspin = uhf ? 3 : 2;
-    // Shell-pair maxima (and their FP32 copies for the precision split).
+    // Shell-pair maxima.
     for (int k = 0; k < nspin; ++k)
     {
-        e->d_smaxf[k].alloc(e->smax_total);
         if (k == 0)
             e->d_smax2.alloc(e->smax_total);
         shell_max_kernel<<<grid_for(e->pairs.size(), 128, e->num_sms), 128, 0, s>>>(
             e->d_dD[k].p, e->d_pairs.p, static_cast<int>(e->pairs.size()), e->d_mat_off.p, e->d_mat_ld.p, e->d_smax_off.p,
-            e->d_nsh.p, e->d_shnao.p, e->d_smax[k].p, k == 0 ? e->d_smax2.p : nullptr, mixed ? e->d_smaxf[k].p : nullptr);
+            e->d_nsh.p, e->d_shnao.p, e->d_smax[k].p, k == 0 ? e->d_smax2.p : nullptr);
         HFG_CUDA(cudaGetLastError());
     }
 
@@ -1195,9 +1190,6 @@ static int build_lists(hfg_engine* e, bool uhf, bool mixed, double sthr, double 
                 a.Mb = uhf ? e->d_smax[2].p : nullptr;
                 a.Qf1 = e->d_cls_Qf[P1].p;
                 a.Qf2 = e->d_cls_Qf[P2].p;
-                a.Mtf = mixed ? e->d_smaxf[0].p : nullptr;
-                a.Maf = mixed ? e->d_smaxf[1].p : nullptr;
-                a.Mbf = (mixed && uhf) ? e->d_smaxf[2].p : nullptr;
                 a.smax_off = e->d_smax_off.p;
                 a.nsh = e->d_nsh.p;
                 a.sthr = sthr;
@@ -1530,7 +1522,6 @@ static void fock_direct(hfg_engine* e, const hfg_fock_request& r, hfg_fock_stats
         e->d_acc[k].alloc(N2);
         e->d_out[k].alloc(N2);
         e->d_smax[k].alloc(e->smax_total);
-        e->d_smaxf[k].alloc(e->smax_total);
         if (mixed && !e->d_dDf[k].p)
         {
             invalidate_graph(e);
@@ -1654,7 +1645,6 @@ static void store_integrals(hfg_engine* e, double sthr, size_t* bytes_out)
         e->d_acc[k].alloc(N2);
         e->d_out[k].alloc(N2);
         e->d_smax[k].alloc(e->smax_total);
-        e->d_smaxf[k].alloc(e->smax_total);
         HFG_CUDA(cudaMemsetAsync(e->d_dD[k].p, 0, sizeof(double) * N2, e->stream));
     }
     e->d_smax2.alloc(e->smax_total);
@@ -2031,7 +2021,7 @@ static double gradient_two_electron(hfg_engine* e, const std::vector<int>& shell
             const int P2 = qc - P1 * (P1 + 1) / 2;
             const int L  = pair_class_l1(P1) + pair_class_l2(P1) + pair_class_l1(P2) + pair_class_l2(P2);
             const void* slice = prec ? static_cast<const void*>(e->d_boys32[L + 1].p) : e->d_boys64[L + 1].p;
-            GradLaunch g {e->d_list[qc][prec].p, n, v[prec], slice, e->d_tables.p, s, e->num_sms, prec == 1};
+            GradLaunch g {e->d_list[qc][prec].p, n, v[prec], slice, e->d_tables.p, s, e->num_sms, prec == 1, e->grad_group_only};
             HFG_CUDA(launch_grad(qc, g));
         }
     HFG_CUDA(cudaEventRecord(e->ev[7], s));
@@ -2494,6 +2484,14 @@ int hfg_set_persistent(hfg_engine* e, int on)
         return HFG_ERR_INVALID;
     hfg::invalidate_graph(e);
     e->persistent = on != 0;
+    return HFG_OK;
+}
+
+int hfg_set_gradient_form(hfg_engine* e, int group_only)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    e->grad_group_only = group_only != 0;
     return HFG_OK;
 }
 

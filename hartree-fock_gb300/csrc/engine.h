@@ -62,6 +62,7 @@ struct GradLaunch
     cudaStream_t stream;
     int num_sms;
     bool fp32;
+    bool group_form; // the lane-group kernel for every class (else the thread form where it is compiled)
 };
 cudaError_t launch_grad(int qclass, const GradLaunch& L);
 

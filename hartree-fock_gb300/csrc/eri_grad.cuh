@@ -331,5 +331,341 @@ __global__ void __launch_bounds__(32 * kGradWarps)
         __syncwarp(gmask);
     }
 }
+
+// Thread-per-quartet form of the gradient for the small classes: every loop over Cartesian components and
+// Hermite indices unrolled at compile time, the per-quartet arrays in registers.  Two passes over the
+// primitive quartets:
+//   bra-outer:  Gs[tuv][kl] = sum_{ket prims} sum_{tau nu phi} (-1)^{tau+nu+phi} E^{kl}_{tau nu phi} R_{t+tau,..}
+//               (t+u+v <= l_ab + 1) accumulates over the ket primitives of one bra primitive pair; then
+//               y[ij][tuv] = sum_kl Gamma_ijkl Gs[tuv][kl] once per bra primitive pair, and
+//               g_A += DA . y,  g_P += E . y(t+1)  (d/dA + d/dB = d/dP: the R index shifted by one);
+//   ket-outer:  Hs[tuv'][ij] = sum_{bra prims} sum_tuv E^{ij}_{tuv} R_{t+tau,..} (tau+nu+phi <= l_cd + 1),
+//               h = sum_ij Gamma_ijkl Hs once per ket primitive pair, g_C += (-1)^{..} DC . h;
+// g_B = g_P - g_A and g_D = -(g_P + g_C).  The Gamma contraction runs once per primitive pair instead of
+// once per primitive quartet; every term whose Hermite index lies outside the non-zero range of its
+// coefficients is dropped at compile time.  Warp-uniform iteration: when the 32 quartets of a warp share
+// the bra pair (bra-sorted lists), g_A and g_B are summed over the warp and added once.
+template <int LA, int LB, int LC, int LD> struct GradThread
+{
+    static constexpr int NAB = ncart(LA) * ncart(LB), NCD = ncart(LC) * ncart(LD);
+    static constexpr int LAB = LA + LB, LCD = LC + LD, L = LAB + LCD + 1;
+    static constexpr int HAB1 = nherm(LAB + 1), HCD1 = nherm(LCD + 1);
+    // Values a thread holds at the peak of either pass (Gamma, R, and the pass's accumulator array).
+    static constexpr int kPass1 = NAB * NCD + nherm(L) + HAB1 * NCD;
+    static constexpr int kPass2 = NAB * NCD + nherm(L) + HCD1 * NAB;
+    static constexpr int kValues = kPass1 > kPass2 ? kPass1 : kPass2;
+};
+
+template <int LA, int LB, int LC, int LD, typename Real>
+__global__ void __launch_bounds__(128)
+    grad_thread_kernel(const Quartet* __restrict__ list, unsigned long long n, GradView v, const Real* __restrict__ boys_slice)
+{
+    using W = GradThread<LA, LB, LC, LD>;
+    constexpr int NB = ncart(LB), ND = ncart(LD), NAB = W::NAB, NCD = W::NCD;
+    constexpr int LAB = W::LAB, LCD = W::LCD, L = W::L, HAB1 = W::HAB1, HCD1 = W::HCD1;
+    constexpr int SB = pp_stride(LA, LB), SK = pp_stride(LC, LD);
+    constexpr int GB = g_stride(LA, LB), GK = g_stride(LC, LD);
+    constexpr int PCB = pair_class(LA, LB), PCK = pair_class(LC, LD);
+    constexpr int G1B = g1d_size(LA, LB), G1K = g1d_size(LC, LD);
+    // 1-D Hermite coefficient E[i][j][t] of a gradient record's axis table (extents l1+2, l2+2, l1+l2+3).
+    constexpr int XB = (LB + 2) * (LAB + 3), YB = LAB + 3, XK = (LD + 2) * (LCD + 3), YK = LCD + 3;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real* slice = reinterpret_cast<Real*>(smem_raw);
+    if (static_cast<unsigned long long>(blockIdx.x) * blockDim.x >= n)
+        return;
+    stage_boys<Real>(boys_slice, slice);
+    const Real* __restrict__ tbf = static_cast<const Real*>(v.pptab[PCB]);
+    const Real* __restrict__ tkf = static_cast<const Real*>(v.pptab[PCK]);
+    const Real* __restrict__ tbg = static_cast<const Real*>(v.gtab[PCB]);
+    const Real* __restrict__ tkg = static_cast<const Real*>(v.gtab[PCK]);
+    const Real* Dt = static_cast<const Real*>(v.Dt);
+    const Real* Da = static_cast<const Real*>(v.Da);
+    const Real* Db = static_cast<const Real*>(v.Db);
+    const int lane = threadIdx.x & 31;
+
+    for (unsigned long long base = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u);
+         base < n; base += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+    {
+        const unsigned long long q = base + lane;
+        const bool active          = q < n;
+        const Quartet qt           = list[active ? q : base];
+        const PairRec bra          = v.pairs[qt.bra];
+        const PairRec ket          = v.pairs[qt.ket];
+        Real gA[3] = {0, 0, 0}, gP[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+        if (active)
+        {
+            const int nn = v.n;
+            const long long a0 = bra.ao1, b0 = bra.ao2, c0 = ket.ao1, d0 = ket.ao2;
+            const Real sdeg = Real(4) * (bra.same ? Real(0.5) : Real(1)) * (ket.same ? Real(0.5) : Real(1)) *
+                              (qt.bra == qt.ket ? Real(0.5) : Real(1));
+            Real Gam[NAB * NCD];
+            static_for<0, NAB * NCD>(
+                [&](auto EE)
+                {
+                    constexpr int e = decltype(EE)::value;
+                    constexpr int ij = e / NCD, kl = e % NCD;
+                    constexpr int i = ij / NB, j = ij % NB, k = kl / ND, l = kl % ND;
+                    constexpr Real an = Real(ang_norm(LA, i) * ang_norm(LB, j) * ang_norm(LC, k) * ang_norm(LD, l));
+                    const long long I = a0 + i, J = b0 + j, K = c0 + k, Lx = d0 + l;
+                    auto D = [&](const Real* M, long long r, long long c) { return M[r + c * nn]; };
+                    const Real g = D(Dt, I, J) * D(Dt, K, Lx) -
+                                   Real(0.5) * (D(Da, I, K) * D(Da, J, Lx) + D(Da, I, Lx) * D(Da, J, K) +
+                                                D(Db, I, K) * D(Db, J, Lx) + D(Db, I, Lx) * D(Db, J, K));
+                    Gam[e] = (sdeg * an) * g;
+                });
+
+            // R^0_{tuv}, t+u+v <= L, of one primitive quartet.
+            auto prim_R = [&](const Real* rb, const Real* rk, Real* R)
+            {
+                const Real p = rb[0], qq = rk[0];
+                const Real X = rb[1] - rk[1], Y = rb[2] - rk[2], Z = rb[3] - rk[3];
+                const Real rs   = hfg_rsqrt(p + qq);
+                const Real rho  = (p * qq) * (rs * rs);
+                const Real pref = (rb[4] * rk[4]) * rs;
+                const Real T    = rho * (X * X + Y * Y + Z * Z);
+                Real F[L + 1];
+                boys_eval<L, Real>(T, slice, F);
+                Real Fs[L + 1];
+                const Real m2r = Real(-2) * rho;
+                Real w         = pref;
+#pragma unroll
+                for (int m = 0; m <= L; ++m)
+                {
+                    Fs[m] = w * F[m];
+                    w *= m2r;
+                }
+                hermite_R<L, Real>(Fs, X, Y, Z, R);
+            };
+
+            // Bra-outer pass: centres A and P.
+            for (int ib = 0; ib < bra.npp; ++ib)
+            {
+                const Real* __restrict__ rb = tbf + static_cast<size_t>(bra.pp_off + ib) * SB;
+                Real Gs[HAB1 * NCD];
+#pragma unroll
+                for (int x = 0; x < HAB1 * NCD; ++x) Gs[x] = Real(0);
+                for (int ik = 0; ik < ket.npp; ++ik)
+                {
+                    const Real* __restrict__ rk = tkf + static_cast<size_t>(ket.pp_off + ik) * SK;
+                    Real R[nherm(L)];
+                    prim_R(rb, rk, R);
+                    static_for<0, NCD>(
+                        [&](auto KL)
+                        {
+                            constexpr int kl   = decltype(KL)::value;
+                            constexpr int lx   = e3_len(LC, LD, kl, 0), ly = e3_len(LC, LD, kl, 1), lz = e3_len(LC, LD, kl, 2);
+                            constexpr int eoff = kPairHeader + e3_offset(LC, LD, kl);
+                            static_for<0, HAB1>(
+                                [&](auto H)
+                                {
+                                    constexpr int h = decltype(H)::value;
+                                    constexpr int t = htuv(h, LAB + 1, 0), u = htuv(h, LAB + 1, 1), w_ = htuv(h, LAB + 1, 2);
+                                    Real s = Real(0);
+                                    static_for<0, lx * ly * lz>(
+                                        [&](auto EE)
+                                        {
+                                            constexpr int e   = decltype(EE)::value;
+                                            constexpr int tau = e % lx, nu = (e / lx) % ly, phi = e / (lx * ly);
+                                            const Real rr   = R[hidx(t + tau, u + nu, w_ + phi, L)];
+                                            const Real term = (LCD == 0) ? rr : rk[eoff + e] * rr;
+                                            if constexpr (((tau + nu + phi) & 1) != 0)
+                                                s -= term;
+                                            else
+                                                s += term;
+                                        });
+                                    Gs[h * NCD + kl] += s;
+                                });
+                        });
+                }
+                const Real* __restrict__ gb = tbg + static_cast<size_t>(bra.pp_off + ib) * GB;
+                const Real a2 = Real(2) * gb[0];
+                const Real* Ex = gb + 2;
+                const Real* Ey = Ex + G1B;
+                const Real* Ez = Ey + G1B;
+                static_for<0, NAB>(
+                    [&](auto IJ)
+                    {
+                        constexpr int ij = decltype(IJ)::value;
+                        constexpr int i = ij / NB, j = ij % NB;
+                        constexpr int ix = cart_exp(LA, i, 0), iy = cart_exp(LA, i, 1), iz = cart_exp(LA, i, 2);
+                        constexpr int jx = cart_exp(LB, j, 0), jy = cart_exp(LB, j, 1), jz = cart_exp(LB, j, 2);
+                        static_for<0, HAB1>(
+                            [&](auto H)
+                            {
+                                constexpr int h = decltype(H)::value;
+                                constexpr int t = htuv(h, LAB + 1, 0), u = htuv(h, LAB + 1, 1), w_ = htuv(h, LAB + 1, 2);
+                                constexpr bool inx = t <= ix + jx + 1 && u <= iy + jy && w_ <= iz + jz;
+                                constexpr bool iny = t <= ix + jx && u <= iy + jy + 1 && w_ <= iz + jz;
+                                constexpr bool inz = t <= ix + jx && u <= iy + jy && w_ <= iz + jz + 1;
+                                if constexpr (inx || iny || inz)
+                                {
+                                    Real y = Real(0);
+#pragma unroll
+                                    for (int kl = 0; kl < NCD; ++kl) y += Gam[ij * NCD + kl] * Gs[h * NCD + kl];
+                                    // E^{ij} along each axis at the index of this term, and its A derivative.
+                                    auto e1 = [](const Real* T, int ii, int jj, int tt, int XS, int YS) { return T[ii * XS + jj * YS + tt]; };
+                                    auto dA = [&](const Real* T, int ii, int jj, int tt)
+                                    {
+                                        Real r = a2 * e1(T, ii + 1, jj, tt, XB, YB);
+                                        if (ii > 0 && tt <= ii - 1 + jj)
+                                            r -= Real(ii) * e1(T, ii - 1, jj, tt, XB, YB);
+                                        return r;
+                                    };
+                                    const Real fx = t <= ix + jx ? e1(Ex, ix, jx, t, XB, YB) : Real(0);
+                                    const Real fy = u <= iy + jy ? e1(Ey, iy, jy, u, XB, YB) : Real(0);
+                                    const Real fz = w_ <= iz + jz ? e1(Ez, iz, jz, w_, XB, YB) : Real(0);
+                                    if constexpr (inx)
+                                    {
+                                        const Real yz = y * fy * fz;
+                                        gA[0] += yz * dA(Ex, ix, jx, t);
+                                        if constexpr (t >= 1)
+                                            gP[0] += yz * e1(Ex, ix, jx, t - 1, XB, YB);
+                                    }
+                                    if constexpr (iny)
+                                    {
+                                        const Real xz = y * fx * fz;
+                                        gA[1] += xz * dA(Ey, iy, jy, u);
+                                        if constexpr (u >= 1)
+                                            gP[1] += xz * e1(Ey, iy, jy, u - 1, XB, YB);
+                                    }
+                                    if constexpr (inz)
+                                    {
+                                        const Real xy = y * fx * fy;
+                                        gA[2] += xy * dA(Ez, iz, jz, w_);
+                                        if constexpr (w_ >= 1)
+                                            gP[2] += xy * e1(Ez, iz, jz, w_ - 1, XB, YB);
+                                    }
+                                }
+                            });
+                    });
+            }
+
+            // Ket-outer pass: centre C.
+            for (int ik = 0; ik < ket.npp; ++ik)
+            {
+                const Real* __restrict__ rk = tkf + static_cast<size_t>(ket.pp_off + ik) * SK;
+                Real Hs[HCD1 * NAB];
+#pragma unroll
+                for (int x = 0; x < HCD1 * NAB; ++x) Hs[x] = Real(0);
+                for (int ib = 0; ib < bra.npp; ++ib)
+                {
+                    const Real* __restrict__ rb = tbf + static_cast<size_t>(bra.pp_off + ib) * SB;
+                    Real R[nherm(L)];
+                    prim_R(rb, rk, R);
+                    static_for<0, NAB>(
+                        [&](auto IJ)
+                        {
+                            constexpr int ij   = decltype(IJ)::value;
+                            constexpr int lx   = e3_len(LA, LB, ij, 0), ly = e3_len(LA, LB, ij, 1), lz = e3_len(LA, LB, ij, 2);
+                            constexpr int eoff = kPairHeader + e3_offset(LA, LB, ij);
+                            static_for<0, HCD1>(
+                                [&](auto H)
+                                {
+                                    constexpr int h   = decltype(H)::value;
+                                    constexpr int tau = htuv(h, LCD + 1, 0), nu = htuv(h, LCD + 1, 1), phi = htuv(h, LCD + 1, 2);
+                                    Real s = Real(0);
+                                    static_for<0, lx * ly * lz>(
+                                        [&](auto EE)
+                                        {
+                                            constexpr int e = decltype(EE)::value;
+                                            constexpr int t = e % lx, u = (e / lx) % ly, w_ = e / (lx * ly);
+                                            const Real rr = R[hidx(t + tau, u + nu, w_ + phi, L)];
+                                            s += (LAB == 0) ? rr : rb[eoff + e] * rr;
+                                        });
+                                    Hs[h * NAB + ij] += s;
+                                });
+                        });
+                }
+                const Real* __restrict__ gk = tkg + static_cast<size_t>(ket.pp_off + ik) * GK;
+                const Real c2 = Real(2) * gk[0];
+                const Real* Ex = gk + 2;
+                const Real* Ey = Ex + G1K;
+                const Real* Ez = Ey + G1K;
+                static_for<0, NCD>(
+                    [&](auto KL)
+                    {
+                        constexpr int kl = decltype(KL)::value;
+                        constexpr int k = kl / ND, l = kl % ND;
+                        constexpr int kx = cart_exp(LC, k, 0), ky = cart_exp(LC, k, 1), kz = cart_exp(LC, k, 2);
+                        constexpr int lx = cart_exp(LD, l, 0), ly = cart_exp(LD, l, 1), lz = cart_exp(LD, l, 2);
+                        static_for<0, HCD1>(
+                            [&](auto H)
+                            {
+                                constexpr int h   = decltype(H)::value;
+                                constexpr int tau = htuv(h, LCD + 1, 0), nu = htuv(h, LCD + 1, 1), phi = htuv(h, LCD + 1, 2);
+                                constexpr bool inx = tau <= kx + lx + 1 && nu <= ky + ly && phi <= kz + lz;
+                                constexpr bool iny = tau <= kx + lx && nu <= ky + ly + 1 && phi <= kz + lz;
+                                constexpr bool inz = tau <= kx + lx && nu <= ky + ly && phi <= kz + lz + 1;
+                                if constexpr (inx || iny || inz)
+                                {
+                                    Real hv = Real(0);
+#pragma unroll
+                                    for (int ij = 0; ij < NAB; ++ij) hv += Gam[ij * NCD + kl] * Hs[h * NAB + ij];
+                                    if constexpr (((tau + nu + phi) & 1) != 0)
+                                        hv = -hv;
+                                    auto e1 = [](const Real* T, int ii, int jj, int tt) { return T[ii * XK + jj * YK + tt]; };
+                                    auto dC = [&](const Real* T, int ii, int jj, int tt)
+                                    {
+                                        Real r = c2 * e1(T, ii + 1, jj, tt);
+                                        if (ii > 0 && tt <= ii - 1 + jj)
+                                            r -= Real(ii) * e1(T, ii - 1, jj, tt);
+                                        return r;
+                                    };
+                                    const Real fx = tau <= kx + lx ? e1(Ex, kx, lx, tau) : Real(0);
+                                    const Real fy = nu <= ky + ly ? e1(Ey, ky, ly, nu) : Real(0);
+                                    const Real fz = phi <= kz + lz ? e1(Ez, kz, lz, phi) : Real(0);
+                                    if constexpr (inx)
+                                        gC[0] += hv * fy * fz * dC(Ex, kx, lx, tau);
+                                    if constexpr (iny)
+                                        gC[1] += hv * fx * fz * dC(Ey, ky, ly, nu);
+                                    if constexpr (inz)
+                                        gC[2] += hv * fx * fy * dC(Ez, kz, lz, phi);
+                                }
+                            });
+                    });
+            }
+        }
+        // g_B = g_P - g_A, g_D = -(g_P + g_C); the bra atoms' terms summed over the warp when it shares the bra.
+        const unsigned bra0 = __shfl_sync(0xffffffffu, qt.bra, 0);
+        const bool bra_warp = __all_sync(0xffffffffu, qt.bra == bra0);
+        Real gB[3], gD[3];
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+        {
+            gB[x] = gP[x] - gA[x];
+            gD[x] = -(gP[x] + gC[x]);
+        }
+        const int ta = v.shell_atom[bra.sh1], tb = v.shell_atom[bra.sh2];
+        if (bra_warp)
+        {
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    gA[x] += __shfl_xor_sync(0xffffffffu, gA[x], o);
+                    gB[x] += __shfl_xor_sync(0xffffffffu, gB[x], o);
+                }
+        }
+        if (bra_warp ? lane == 0 : active)
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+            {
+                atomicAdd(v.grad + 3 * ta + x, widen(gA[x]));
+                atomicAdd(v.grad + 3 * tb + x, widen(gB[x]));
+            }
+        if (active)
+        {
+            const int tc = v.shell_atom[ket.sh1], td = v.shell_atom[ket.sh2];
+#pragma unroll
+            for (int x = 0; x < 3; ++x)
+            {
+                atomicAdd(v.grad + 3 * tc + x, widen(gC[x]));
+                atomicAdd(v.grad + 3 * td + x, widen(gD[x]));
+            }
+        }
+    }
+}
 #endif
 } // namespace hfg

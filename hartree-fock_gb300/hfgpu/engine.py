@@ -108,6 +108,7 @@ def lib():
         L.hfg_set_primitive_threshold.argtypes = [vp, ctypes.c_double]
         L.hfg_set_graph_mode.argtypes = [vp, ip]
         L.hfg_set_persistent.argtypes = [vp, ip]
+        L.hfg_set_gradient_form.argtypes = [vp, ip]
         L.hfg_set_precision_overlap.argtypes = [vp, ip, ctypes.c_double]
         L.hfg_set_precision_shares.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.hfg_kernel_forms.argtypes = [vp, ip, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)]
@@ -301,6 +302,10 @@ class Engine:
     def set_persistent(self, on: bool):
         """Run the small classes of both precisions as one persistent work-queue launch."""
         self._check(lib().hfg_set_persistent(self.h, 1 if on else 0))
+
+    def set_gradient_form(self, group_only: bool):
+        """Gradient kernels: the lane-group form for every class (True) or the thread form where compiled."""
+        self._check(lib().hfg_set_gradient_form(self.h, 1 if group_only else 0))
 
     def set_primitive_threshold(self, threshold: float):
         """Primitive-pair screening of the Fock build (0 keeps every primitive pair; default 1e-15)."""

@@ -185,6 +185,12 @@ int hfg_set_graph_mode(hfg_engine* engine, int on);
  * rounding (the digestion's atomics sum in a different order). */
 int hfg_set_persistent(hfg_engine* engine, int on);
 
+/* Gradient kernel form (no reference counterpart): 0 (default) runs the thread-per-quartet gradient kernel
+ * for the classes whose per-quartet arrays fit in registers ((ss|ss) (ps|ss) (ps|ps) (pp|ss) (ds|ss) in
+ * FP64, and (pp|ps) (ds|ps) (dp|ss) as well in FP32) and the lane-group kernel for the others; 1 runs the
+ * lane-group kernel for every class.  Both give the same gradient to rounding. */
+int hfg_set_gradient_form(hfg_engine* engine, int group_only);
+
 /* Forms in use: forms[qc] for the given precision and spin case, 0 where AUTO has not decided yet.
  * `available` (may be NULL) receives the bit mask of compiled forms per class (bit f = form f). */
 int hfg_kernel_forms(hfg_engine* engine, int fp32, int unrestricted, int forms[HFG_NUM_CLASSES],
