@@ -106,25 +106,32 @@ template <typename Real, bool UHF> cudaError_t launch_t(const ClassLaunch& c)
     {
         if (form == kFormChunk)
         {
+            // One launch per chunk of kChunk ket components, each over the whole list.
             constexpr int nch = num_chunks<LC, LD, kChunk>();
-            auto kern         = jk_class_chunk_kernel<LA, LB, LC, LD, Real, UHF, kChunk>;
-            const size_t smem = slice_bytes;
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-            if (e != cudaSuccess)
-                return e;
-            int per_sm = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
-            if (e != cudaSuccess)
-                return e;
-            // Quartet blocks of 128; every one is NCH consecutive blocks (one per chunk).
-            const unsigned long long need = (c.count_host + 127) / 128;
-            unsigned long long cap = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share) / nch;
-            if (cap < 1)
-                cap = 1;
-            const unsigned long long qblocks = need < cap ? need : cap;
-            kern<<<static_cast<unsigned>(qblocks * nch), 128, smem, c.stream>>>(c.list, c.count_dev, c.view,
-                                                                                  static_cast<const Real*>(c.boys_slice));
-            return cudaGetLastError();
+            cudaError_t err   = cudaSuccess;
+            static_for<0, nch>(
+                [&](auto C)
+                {
+                    constexpr int k0 = decltype(C)::value * kChunk;
+                    constexpr int k1 = k0 + kChunk < NCD ? k0 + kChunk : NCD;
+                    if (err != cudaSuccess)
+                        return;
+                    auto kern         = jk_class_chunk_kernel<LA, LB, LC, LD, Real, UHF, k0, k1>;
+                    const size_t smem = slice_bytes;
+                    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+                    if (err != cudaSuccess)
+                        return;
+                    int per_sm = 0;
+                    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
+                    if (err != cudaSuccess)
+                        return;
+                    const unsigned long long need = (c.count_host + 127) / 128;
+                    const unsigned long long cap  = static_cast<unsigned long long>(c.num_sms) * resident(per_sm, c.share);
+                    kern<<<static_cast<unsigned>(need < cap ? need : cap), 128, smem, c.stream>>>(
+                        c.list, c.count_dev, c.view, static_cast<const Real*>(c.boys_slice));
+                    err = cudaGetLastError();
+                });
+            return err;
         }
     }
     constexpr bool kHasWarp = kWarpForm || dual_form(sizeof(Real) == 4);
@@ -203,9 +210,11 @@ cudaError_t HFG_CAT(launch_stored_, HFG_QCLASS)(const StoredLaunch& c)
     return cudaGetLastError();
 }
 
+// Bits 0-15: compiled forms; 16-23: the default form; 24-31: kernel launches of one chunk-form launch.
 unsigned HFG_CAT(class_form_mask_, HFG_QCLASS)(bool fp32)
 {
-    return form_mask(fp32) | (static_cast<unsigned>(default_form(fp32)) << 16);
+    const unsigned nch = chunk_width(fp32) > 0 ? static_cast<unsigned>((NCD + chunk_width(fp32) - 1) / chunk_width(fp32)) : 0u;
+    return form_mask(fp32) | (static_cast<unsigned>(default_form(fp32)) << 16) | (nch << 24);
 }
 #elif HFG_PART == 1
 cudaError_t HFG_CAT(launch_class32_, HFG_QCLASS)(const ClassLaunch& c)

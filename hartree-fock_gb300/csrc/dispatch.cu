@@ -66,7 +66,8 @@ static unsigned (*const kMask[kNumQuartetClasses])(bool) = {
     class_form_mask_15, class_form_mask_16, class_form_mask_17, class_form_mask_18, class_form_mask_19,
     class_form_mask_20};
 
-// The class TUs return the compiled-form mask in bits 0-15 and the default form in bits 16-23.
+// The class TUs return the compiled-form mask in bits 0-15, the default form in bits 16-23 and the
+// kernel launches of the chunk form (one per chunk) in bits 24-31.
 unsigned class_form_mask(int qclass, bool fp32)
 {
     return (qclass >= 0 && qclass < kNumQuartetClasses) ? (kMask[qclass](fp32) & 0xffffu) : 0u;
@@ -75,6 +76,16 @@ unsigned class_form_mask(int qclass, bool fp32)
 int class_default_form(int qclass, bool fp32)
 {
     return (qclass >= 0 && qclass < kNumQuartetClasses) ? static_cast<int>((kMask[qclass](fp32) >> 16) & 0xffu) : 0;
+}
+
+int class_launches(int qclass, bool fp32, int form)
+{
+    if (qclass < 0 || qclass >= kNumQuartetClasses)
+        return 0;
+    const unsigned m = kMask[qclass](fp32);
+    if (form == 0)
+        form = static_cast<int>((m >> 16) & 0xffu);
+    return form == kFormChunk ? static_cast<int>((m >> 24) & 0xffu) : 1;
 }
 
 } // namespace hfg

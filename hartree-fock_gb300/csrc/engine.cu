@@ -1443,7 +1443,7 @@ static int enqueue_build(hfg_engine* e, const hfg_fock_request& r, bool graph, i
                 c.form = pick_form(e, qc, prec, uhf, c, ms_tune);
             HFG_CUDA(launch_class(qc, c));
             form_ran[qc][prec] = c.form != 0 ? c.form : class_default_form(qc, prec == 1);
-            ++launches;
+            launches += class_launches(qc, prec == 1, c.form);
         }
         if (!graph && overlap && prec == 1)
             HFG_CUDA(cudaEventRecord(e->ev2[3], ps));

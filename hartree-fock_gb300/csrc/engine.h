@@ -37,6 +37,8 @@ cudaError_t launch_class(int qclass, const ClassLaunch& L);
 unsigned class_form_mask(int qclass, bool fp32);
 // The form a launch with form == 0 runs.
 int class_default_form(int qclass, bool fp32);
+// Kernel launches one launch_class call makes in the given form (0: the default form).
+int class_launches(int qclass, bool fp32, int form);
 
 // Digestion of one class's stored integrals (the stored-integral SCF).
 struct StoredLaunch

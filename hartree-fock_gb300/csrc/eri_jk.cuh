@@ -564,10 +564,13 @@ __global__ void __launch_bounds__(128) jk_class_kernel(const Quartet* __restrict
 // d-containing classes a thread cannot hold a whole quartet's G[HAB][NCD] and ERI[NAB][NCD] in registers;
 // restricted to CH ket components the thread keeps R, G[HAB][CH] and ERI[NAB][CH] in registers, with every
 // loop unrolled at compile time, and digests the integrals of its chunk (the bra Coulomb block summed over
-// the warp as in the thread form; the exchange and ket Coulomb elements its chunk reaches).  The chunks
-// of a quartet run in neighbouring blocks (block b: chunk b % NCH), so they share the quartet's records in
-// L1/L2.  Each chunk recomputes the Boys values and R of its quartet: for FP32, where these are cheap
-// next to the two Hermite transforms, that buys full lanes and no shared-memory round trips.
+// the warp as in the thread form; the exchange and ket Coulomb elements its chunk reaches).  Each chunk
+// is its own launch over the whole list (jk_class_chunk_kernel<..., KL0, KL1>), so that every SM runs one
+// chunk's unrolled code at a time: with the chunks of a quartet in neighbouring blocks of one launch the
+// resident blocks of an SM ran different chunk bodies and stalled on instruction fetch (ncu: 30 cycles
+// per issued instruction).  Each chunk recomputes the Boys values and R of its quartet: for FP32, where
+// these are cheap next to the two Hermite transforms, that buys full lanes and no shared-memory round
+// trips; the list and the records are re-read per chunk from L2.
 template <int LA, int LB, int LC, int LD, typename Real, bool UHF, int KL0, int KL1>
 __device__ __forceinline__ void chunk_body(const Quartet* __restrict__ list, unsigned long long n, const FockView& v,
                                            const Real* __restrict__ slice, unsigned qb, unsigned nqb)
@@ -621,34 +624,25 @@ __device__ __forceinline__ void chunk_body(const Quartet* __restrict__ list, uns
     }
 }
 
-// Blocks of the chunked form: NCH consecutive blocks hold the NCH chunks of the same 128 quartets.
+// Chunks of CH ket components of a (LC LD) ket.
 template <int LC, int LD, int CH> __host__ __device__ constexpr int num_chunks()
 {
     return (ncart(LC) * ncart(LD) + CH - 1) / CH;
 }
 
-template <int LA, int LB, int LC, int LD, typename Real, bool UHF, int CH>
+// One chunk, ket components [KL0, KL1), of every quartet of the list.
+template <int LA, int LB, int LC, int LD, typename Real, bool UHF, int KL0, int KL1>
 __global__ void __launch_bounds__(128) jk_class_chunk_kernel(const Quartet* __restrict__ list,
                                                              const unsigned long long* __restrict__ count, FockView v,
                                                              const Real* __restrict__ boys_slice)
 {
-    constexpr int NCD = ncart(LC) * ncart(LD), NCH = num_chunks<LC, LD, CH>();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Real* slice                = reinterpret_cast<Real*>(smem_raw);
     const unsigned long long n = *count;
-    const unsigned qb = blockIdx.x / NCH, nqb = gridDim.x / NCH;
-    const int chunk   = static_cast<int>(blockIdx.x % NCH);
-    if (qb >= nqb || static_cast<unsigned long long>(qb) * blockDim.x >= n)
+    if (static_cast<unsigned long long>(blockIdx.x) * blockDim.x >= n)
         return;
     stage_boys<Real>(boys_slice, slice);
-    static_for<0, NCH>(
-        [&](auto C)
-        {
-            constexpr int c = decltype(C)::value;
-            if (chunk == c)
-                chunk_body<LA, LB, LC, LD, Real, UHF, c * CH, (c * CH + CH < NCD ? c * CH + CH : NCD)>(list, n, v, slice,
-                                                                                                      qb, nqb);
-        });
+    chunk_body<LA, LB, LC, LD, Real, UHF, KL0, KL1>(list, n, v, slice, blockIdx.x, gridDim.x);
 }
 
 // Digestion of stored integrals (the stored-integral SCF): integral blocks written once in store mode
