@@ -9,12 +9,16 @@
 //
 // Centre derivatives in McMurchie-Davidson form: d/dA_x of a primitive pair distribution has Hermite
 // coefficients  DA^{ij}_t = 2a E^{i+1,j}_t - i E^{i-1,j}_t  (x factor; y and z factors unchanged), likewise
-// DB with b and j, DC/DD on the ket.  The kernel never forms derivative integrals: per primitive quartet
-//   G[tuv][kl]  = sum_{tau nu phi} (-1)^{tau+nu+phi} E^{kl}_{tau nu phi} R_{t+tau,..}   (t+u+v <= l_ab + 1)
-//   y[ij][tuv]  = sum_kl Gamma_ijkl G[tuv][kl]          -> g_A += DA . y,  g_B += DB . y
-//   X[ij][tuv'] = sum_{tuv} E^{ij}_{tuv} R_{t+tau,..}   (tau+nu+phi <= l_cd + 1)
-//   h[kl][tuv'] = sum_ij Gamma_ijkl X[ij][tuv']         -> g_C += (-1)^{..} DC . h
-// and g_D = -(g_A + g_B + g_C) (translational invariance).  E/R tables are recomputed here, nothing from
+// DB with b and j, DC/DD on the ket.  The kernels never form derivative integrals; in two passes over
+// the primitive quartets of a shell quartet
+//   bra-outer: G[tuv][kl]  = sum_{ket prims} sum_{tau nu phi} (-1)^{tau+nu+phi} E^{kl}_{tau nu phi} R_{t+tau,..}
+//              (t+u+v <= l_ab + 1), then once per bra primitive pair
+//              y[ij][tuv]  = sum_kl Gamma_ijkl G[tuv][kl]          -> g_A += DA . y,  g_B += DB . y
+//   ket-outer: X[ij][tuv'] = sum_{bra prims} sum_{tuv} E^{ij}_{tuv} R_{t+tau,..}   (tau+nu+phi <= l_cd + 1),
+//              then once per ket primitive pair
+//              h[kl][tuv'] = sum_ij Gamma_ijkl X[ij][tuv']         -> g_C += (-1)^{..} DC . h
+// and g_D = -(g_A + g_B + g_C) (translational invariance): the Gamma contractions run once per primitive
+// pair, not once per primitive quartet, at the price of evaluating R twice.  E/R tables are recomputed here, nothing from
 // the forward build is stored.  FP64, or FP32 for the small-bound quartets of a mixed-precision gradient
 // (FP64 accumulation).  One group of lanes per quartet (GradLayout::kGroup: 4 to 32 lanes by
 // class size; the groups of a warp work independently, synchronised by group masks).
@@ -136,71 +140,78 @@ __global__ void __launch_bounds__(32 * kGradWarps)
         __syncwarp(gmask);
         Real gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
 
+        // R^0_{tuv} of one primitive quartet into one of the group's two R buffers (levels in parallel over
+        // the group's lanes); returns the buffer that holds it.
+        auto group_R = [&](const Real* rb, const Real* rk) -> const Real*
+        {
+            const Real p = rb[0], qq = rk[0];
+            const Real X = rb[1] - rk[1], Y = rb[2] - rk[2], Z = rb[3] - rk[3];
+            const Real rs   = hfg_rsqrt(p + qq);
+            const Real rho  = (p * qq) * (rs * rs);
+            const Real pref = (rb[4] * rk[4]) * rs;
+            const Real T    = rho * (X * X + Y * Y + Z * Z);
+            Real F[L + 1];
+            boys_eval<L, Real>(T, slice, F);
+            Real Fs[L + 1];
+            {
+                const Real m2r = Real(-2) * rho;
+                Real w         = pref;
+#pragma unroll
+                for (int k = 0; k <= L; ++k)
+                {
+                    Fs[k] = w * F[k];
+                    w *= m2r;
+                }
+            }
+            Real* src = Rbuf0;
+            Real* dst = Rbuf1;
+            if (lane == 0)
+                src[0] = Fs[L];
+            __syncwarp(gmask);
+#pragma unroll
+            for (int lev = L - 1; lev >= 0; --lev)
+            {
+                const int cnt = nherm(L - lev);
+                for (int k = 1 + lane; k < cnt; k += GS)
+                {
+                    const int4 r  = tabs->rtab[L][k];
+                    const int ax  = r.w & 3, c = r.w >> 2;
+                    const Real xa = ax == 0 ? X : (ax == 1 ? Y : Z);
+                    Real val    = xa * src[r.y];
+                    if (c > 0)
+                    {
+                        if constexpr (sizeof(Real) == 8)
+                            val = fma(tabs->rcoef[L][k], src[r.z], val);
+                        else
+                            val = fmaf(Real(c), src[r.z], val);
+                    }
+                    dst[r.x] = val;
+                }
+                if (lane == 0)
+                    dst[0] = Fs[lev];
+                __syncwarp(gmask);
+                Real* t = src;
+                src       = dst;
+                dst       = t;
+            }
+            return src;
+        };
+
+        // Bra-outer pass (centres A, B): G[tuv][kl] (t+u+v <= LAB+1) summed over the ket primitives of one
+        // bra primitive pair, then contracted with Gamma and the bra's derivative coefficients once per bra
+        // primitive pair.
         for (int ib = 0; ib < bra.npp; ++ib)
         {
             const Real* __restrict__ rb = static_cast<const Real*>(v.pptab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * SB;
             const Real* __restrict__ gb = static_cast<const Real*>(v.gtab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * GB;
-            const Real p = rb[0], Px = rb[1], Py = rb[2], Pz = rb[3], Wab = rb[4];
             const Real aexp = gb[0], bexp = gb[1];
+            for (int e = lane; e < HAB1 * NCD; e += GS) Gs[e] = Real(0);
             for (int ik = 0; ik < ket.npp; ++ik)
             {
                 const Real* __restrict__ rk = static_cast<const Real*>(v.pptab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * SK;
                 const Real* __restrict__ gk = static_cast<const Real*>(v.gtab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * GK;
-                const Real qq = rk[0];
-                const Real X = Px - rk[1], Y = Py - rk[2], Z = Pz - rk[3];
-                const Real rs   = hfg_rsqrt(p + qq);
-                const Real rho  = (p * qq) * (rs * rs);
-                const Real pref = (Wab * rk[4]) * rs;
-                const Real T    = rho * (X * X + Y * Y + Z * Z);
-                const Real cexp = gk[0];
-                Real F[L + 1];
-                boys_eval<L, Real>(T, slice, F);
-                Real Fs[L + 1];
-                {
-                    const Real m2r = Real(-2) * rho;
-                    Real w         = pref;
-#pragma unroll
-                    for (int k = 0; k <= L; ++k)
-                    {
-                        Fs[k] = w * F[k];
-                        w *= m2r;
-                    }
-                }
-                Real* src = Rbuf0;
-                Real* dst = Rbuf1;
-                if (lane == 0)
-                    src[0] = Fs[L];
-                __syncwarp(gmask);
-#pragma unroll
-                for (int lev = L - 1; lev >= 0; --lev)
-                {
-                    const int cnt = nherm(L - lev);
-                    for (int k = 1 + lane; k < cnt; k += GS)
-                    {
-                        const int4 r  = tabs->rtab[L][k];
-                        const int ax  = r.w & 3, c = r.w >> 2;
-                        const Real xa = ax == 0 ? X : (ax == 1 ? Y : Z);
-                        Real val    = xa * src[r.y];
-                        if (c > 0)
-                        {
-                            if constexpr (sizeof(Real) == 8)
-                                val = fma(tabs->rcoef[L][k], src[r.z], val);
-                            else
-                                val = fmaf(Real(c), src[r.z], val);
-                        }
-                        dst[r.x] = val;
-                    }
-                    if (lane == 0)
-                        dst[0] = Fs[lev];
-                    __syncwarp(gmask);
-                    Real* t = src;
-                    src       = dst;
-                    dst       = t;
-                }
-                const Real* R = src;
+                const Real* R = group_R(rb, rk);
                 auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
-
-                // G[tuv][kl] over t+u+v <= LAB+1, and X[ij][tuv'] over t+u+v <= LCD+1.
                 for (int e = lane; e < HAB1 * NCD; e += GS)
                 {
                     const int h = e / NCD, kl = e % NCD;
@@ -223,8 +234,57 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                                 s = fma(((ta + nu + ph) & 1) ? -ek : ek, Ridx(t + ta, u + nu, w_ + ph), s);
                             }
                         }
-                    Gs[e] = s;
+                    Gs[e] += s;
                 }
+                __syncwarp(gmask); // G read R; the next primitive quartet overwrites the R buffers
+            }
+            for (int e = lane; e < NAB * HAB1; e += GS)
+            {
+                const int ij = e / HAB1, h = e % HAB1;
+                Real y = Real(0);
+                for (int kl = 0; kl < NCD; ++kl) y += Gam[ij * NCD + kl] * Gs[h * NCD + kl];
+                if (y == Real(0))
+                    continue;
+                const int tuv = tabs->htuv[LAB + 1][h];
+                const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
+                const int i = ij / NB, j = ij % NB;
+                const int ie[3] = {cart_exp(LA, i, 0), cart_exp(LA, i, 1), cart_exp(LA, i, 2)};
+                const int je[3] = {cart_exp(LB, j, 0), cart_exp(LB, j, 1), cart_exp(LB, j, 2)};
+                const Real* E[3] = {gb + 2, gb + 2 + G1B, gb + 2 + 2 * G1B};
+                Real f[3], dA[3], dB[3];
+                for (int x = 0; x < 3; ++x)
+                {
+                    const int t = tt[x];
+                    f[x]  = (t <= ie[x] + je[x]) ? e1(E[x], LB, LAB, ie[x], je[x], t) : Real(0);
+                    dA[x] = Real(2) * aexp * e1(E[x], LB, LAB, ie[x] + 1, je[x], t) -
+                            (ie[x] > 0 ? ie[x] * e1(E[x], LB, LAB, ie[x] - 1, je[x], t) : Real(0));
+                    dB[x] = Real(2) * bexp * e1(E[x], LB, LAB, ie[x], je[x] + 1, t) -
+                            (je[x] > 0 ? je[x] * e1(E[x], LB, LAB, ie[x], je[x] - 1, t) : Real(0));
+                }
+                gA[0] += y * dA[0] * f[1] * f[2];
+                gA[1] += y * f[0] * dA[1] * f[2];
+                gA[2] += y * f[0] * f[1] * dA[2];
+                gB[0] += y * dB[0] * f[1] * f[2];
+                gB[1] += y * f[0] * dB[1] * f[2];
+                gB[2] += y * f[0] * f[1] * dB[2];
+            }
+            __syncwarp(gmask); // the contraction read Gs before the next bra primitive pair clears it
+        }
+
+        // Ket-outer pass (centre C): X[ij][tuv'] (tau+nu+phi <= LCD+1) summed over the bra primitives of one
+        // ket primitive pair, then contracted once per ket primitive pair.
+        for (int ik = 0; ik < ket.npp; ++ik)
+        {
+            const Real* __restrict__ rk = static_cast<const Real*>(v.pptab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * SK;
+            const Real* __restrict__ gk = static_cast<const Real*>(v.gtab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * GK;
+            const Real cexp = gk[0];
+            for (int e = lane; e < NAB * HCD1; e += GS) Xs[e] = Real(0);
+            for (int ib = 0; ib < bra.npp; ++ib)
+            {
+                const Real* __restrict__ rb = static_cast<const Real*>(v.pptab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * SB;
+                const Real* __restrict__ gb = static_cast<const Real*>(v.gtab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * GB;
+                const Real* R = group_R(rb, rk);
+                auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
                 for (int e = lane; e < NAB * HCD1; e += GS)
                 {
                     const int ij = e / HCD1, h = e % HCD1;
@@ -244,70 +304,38 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                             for (int t = 0; t <= ix + jx; ++t)
                                 s += eyz * e1(Ex, LB, LAB, ix, jx, t) * Ridx(t + ta, u + nu, w_ + ph);
                         }
-                    Xs[e] = s;
-                }
-                __syncwarp(gmask);
-                // Bra centres A, B.
-                for (int e = lane; e < NAB * HAB1; e += GS)
-                {
-                    const int ij = e / HAB1, h = e % HAB1;
-                    Real y = Real(0);
-                    for (int kl = 0; kl < NCD; ++kl) y += Gam[ij * NCD + kl] * Gs[h * NCD + kl];
-                    if (y == Real(0))
-                        continue;
-                    const int tuv = tabs->htuv[LAB + 1][h];
-                    const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
-                    const int i = ij / NB, j = ij % NB;
-                    const int ie[3] = {cart_exp(LA, i, 0), cart_exp(LA, i, 1), cart_exp(LA, i, 2)};
-                    const int je[3] = {cart_exp(LB, j, 0), cart_exp(LB, j, 1), cart_exp(LB, j, 2)};
-                    const Real* E[3] = {gb + 2, gb + 2 + G1B, gb + 2 + 2 * G1B};
-                    Real f[3], dA[3], dB[3];
-                    for (int x = 0; x < 3; ++x)
-                    {
-                        const int t = tt[x];
-                        f[x]  = (t <= ie[x] + je[x]) ? e1(E[x], LB, LAB, ie[x], je[x], t) : Real(0);
-                        dA[x] = Real(2) * aexp * e1(E[x], LB, LAB, ie[x] + 1, je[x], t) -
-                                (ie[x] > 0 ? ie[x] * e1(E[x], LB, LAB, ie[x] - 1, je[x], t) : Real(0));
-                        dB[x] = Real(2) * bexp * e1(E[x], LB, LAB, ie[x], je[x] + 1, t) -
-                                (je[x] > 0 ? je[x] * e1(E[x], LB, LAB, ie[x], je[x] - 1, t) : Real(0));
-                    }
-                    gA[0] += y * dA[0] * f[1] * f[2];
-                    gA[1] += y * f[0] * dA[1] * f[2];
-                    gA[2] += y * f[0] * f[1] * dA[2];
-                    gB[0] += y * dB[0] * f[1] * f[2];
-                    gB[1] += y * f[0] * dB[1] * f[2];
-                    gB[2] += y * f[0] * f[1] * dB[2];
-                }
-                // Ket centre C.
-                for (int e = lane; e < NCD * HCD1; e += GS)
-                {
-                    const int kl = e / HCD1, h = e % HCD1;
-                    Real hv = Real(0);
-                    for (int ij = 0; ij < NAB; ++ij) hv += Gam[ij * NCD + kl] * Xs[ij * HCD1 + h];
-                    if (hv == Real(0))
-                        continue;
-                    const int tuv = tabs->htuv[LCD + 1][h];
-                    const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
-                    if ((tt[0] + tt[1] + tt[2]) & 1)
-                        hv = -hv;
-                    const int k = kl / ND, l = kl % ND;
-                    const int ke[3] = {cart_exp(LC, k, 0), cart_exp(LC, k, 1), cart_exp(LC, k, 2)};
-                    const int le[3] = {cart_exp(LD, l, 0), cart_exp(LD, l, 1), cart_exp(LD, l, 2)};
-                    const Real* E[3] = {gk + 2, gk + 2 + G1K, gk + 2 + 2 * G1K};
-                    Real f[3], dC[3];
-                    for (int x = 0; x < 3; ++x)
-                    {
-                        const int t = tt[x];
-                        f[x]  = (t <= ke[x] + le[x]) ? e1(E[x], LD, LCD, ke[x], le[x], t) : Real(0);
-                        dC[x] = Real(2) * cexp * e1(E[x], LD, LCD, ke[x] + 1, le[x], t) -
-                                (ke[x] > 0 ? ke[x] * e1(E[x], LD, LCD, ke[x] - 1, le[x], t) : Real(0));
-                    }
-                    gC[0] += hv * dC[0] * f[1] * f[2];
-                    gC[1] += hv * f[0] * dC[1] * f[2];
-                    gC[2] += hv * f[0] * f[1] * dC[2];
+                    Xs[e] += s;
                 }
                 __syncwarp(gmask);
             }
+            for (int e = lane; e < NCD * HCD1; e += GS)
+            {
+                const int kl = e / HCD1, h = e % HCD1;
+                Real hv = Real(0);
+                for (int ij = 0; ij < NAB; ++ij) hv += Gam[ij * NCD + kl] * Xs[ij * HCD1 + h];
+                if (hv == Real(0))
+                    continue;
+                const int tuv = tabs->htuv[LCD + 1][h];
+                const int tt[3] = {tuv & 255, (tuv >> 8) & 255, tuv >> 16};
+                if ((tt[0] + tt[1] + tt[2]) & 1)
+                    hv = -hv;
+                const int k = kl / ND, l = kl % ND;
+                const int ke[3] = {cart_exp(LC, k, 0), cart_exp(LC, k, 1), cart_exp(LC, k, 2)};
+                const int le[3] = {cart_exp(LD, l, 0), cart_exp(LD, l, 1), cart_exp(LD, l, 2)};
+                const Real* E[3] = {gk + 2, gk + 2 + G1K, gk + 2 + 2 * G1K};
+                Real f[3], dC[3];
+                for (int x = 0; x < 3; ++x)
+                {
+                    const int t = tt[x];
+                    f[x]  = (t <= ke[x] + le[x]) ? e1(E[x], LD, LCD, ke[x], le[x], t) : Real(0);
+                    dC[x] = Real(2) * cexp * e1(E[x], LD, LCD, ke[x] + 1, le[x], t) -
+                            (ke[x] > 0 ? ke[x] * e1(E[x], LD, LCD, ke[x] - 1, le[x], t) : Real(0));
+                }
+                gC[0] += hv * dC[0] * f[1] * f[2];
+                gC[1] += hv * f[0] * dC[1] * f[2];
+                gC[2] += hv * f[0] * f[1] * dC[2];
+            }
+            __syncwarp(gmask);
         }
         for (int x = 0; x < 3; ++x)
             for (int o = GS / 2; o > 0; o >>= 1)
