@@ -61,6 +61,8 @@ def parse_args():
     ap.add_argument("--fp32-cutoff", type=float, default=1e-4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of one baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="default kernel form per class, no form-timing trials (the same launches with or without a profiler)")
     ap.add_argument("--scf", action="store_true",
                     help="also time the UHF SCFs and the FP64 gradient (the RHF SCFs and the mixed gradient always run at N=1)")
     ap.add_argument("--no-scf", action="store_true", help="skip the SCF and gradient timings")
@@ -308,6 +310,8 @@ def gpu_arm(args, dist):
     torch.cuda.set_device(dev)
     Z, xyz, soa = make_workload(args.workload)
     eng = Engine(soa, device=dev)
+    if args.no_tune:
+        eng.set_autotune(False)
     Da, _ = eng.core_guess(Z, xyz, 0, 1)
     n = eng.nao
     t64 = lambda a: torch.from_numpy(np.asfortranarray(a).ravel(order="F")).to(f"cuda:{dev}")
@@ -399,7 +403,8 @@ def gpu_arm(args, dist):
             "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (seeded water lattice, core-guess density)",
             "config": {"workload": WORKLOADS[args.workload]["name"], "precision": "mixed FP32/FP64",
                        "fp32_cutoff": args.fp32_cutoff, "schwartz_thresh": 1e-10, "density_thresh": 1e-10,
-                       "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas x{dist.world}"},
+                       "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas x{dist.world}",
+                       "kernel_forms": "class defaults (--no-tune)" if args.no_tune else "autotuned on first use"},
             "fp64_builds_per_s": fp64_value,
             "speedup_mixed_vs_fp64": value / fp64_value if fp64_value else None,
             "delta_e2_mixed_vs_fp64": abs(e2_mixed - e2_fp64),

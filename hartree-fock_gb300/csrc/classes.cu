@@ -52,11 +52,13 @@ constexpr int chunk_width(bool fp32)
         return 0;
     return (QC == 12 || QC == 13) ? 3 : QC == 14 ? 2 : (QC >= 16 && QC <= 19) ? 1 : 0;
 }
-// The form a launch with form 0 runs (before or without autotuning): the chunked form where it measured
-// fastest at full size ((H2O)_64/6-31G**: (dp|dp), (dd|pp), (dd|ds), (dd|dp) in FP32), else warp or thread.
+// The form a launch with form 0 runs (before or without autotuning): the chunked form where the tuner
+// keeps it at full size ((H2O)_64/6-31G**: (dp|pp), (dp|ds), (dp|dp), (dd|pp), (dd|ds), (dd|dp) in FP32),
+// else warp or thread.
 constexpr int default_form(bool fp32)
 {
-    return (fp32 && (QC == 14 || (QC >= 17 && QC <= 19))) ? kFormChunk : (warp_form(fp32) ? kFormWarp : kFormThread);
+    return (fp32 && (QC == 12 || QC == 13 || QC == 14 || (QC >= 17 && QC <= 19))) ? kFormChunk
+                                                                                   : (warp_form(fp32) ? kFormWarp : kFormThread);
 }
 constexpr unsigned form_mask(bool fp32)
 {

@@ -249,6 +249,8 @@ struct hfg_engine
     hfg::DevBuf<unsigned long long> d_pcounter;
     // Gradient kernels: the lane-group form for every class (hfg_set_gradient_form).
     bool grad_group_only = false;
+    // Kernel-form autotuning on first use of a class (hfg_set_autotune); off: default forms only.
+    bool autotune = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     struct GraphKey
@@ -1261,8 +1263,8 @@ int pick_form(hfg_engine* e, int qc, int prec, bool uhf, const ClassLaunch& base
         return pick;
     }
     const unsigned long long n = base.count_host;
-    if (n < kTuneMin)
-        return 0; // too small to time; the default form runs and the class stays untuned
+    if (n < kTuneMin || !e->autotune)
+        return 0; // too small to time, or tuning off: the default form runs and the class stays untuned
     const auto t0 = std::chrono::steady_clock::now();
     const unsigned long long nch   = n <= kTuneSample ? 1 : kTuneChunks;
     const unsigned long long chunk = n <= kTuneSample ? n : kTuneSample / kTuneChunks;
@@ -2484,6 +2486,14 @@ int hfg_set_persistent(hfg_engine* e, int on)
         return HFG_ERR_INVALID;
     hfg::invalidate_graph(e);
     e->persistent = on != 0;
+    return HFG_OK;
+}
+
+int hfg_set_autotune(hfg_engine* e, int on)
+{
+    if (!e)
+        return HFG_ERR_INVALID;
+    e->autotune = on != 0;
     return HFG_OK;
 }
 

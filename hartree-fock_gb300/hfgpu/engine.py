@@ -109,6 +109,7 @@ def lib():
         L.hfg_set_graph_mode.argtypes = [vp, ip]
         L.hfg_set_persistent.argtypes = [vp, ip]
         L.hfg_set_gradient_form.argtypes = [vp, ip]
+        L.hfg_set_autotune.argtypes = [vp, ip]
         L.hfg_set_precision_overlap.argtypes = [vp, ip, ctypes.c_double]
         L.hfg_set_precision_shares.argtypes = [vp, ctypes.c_double, ctypes.c_double]
         L.hfg_kernel_forms.argtypes = [vp, ip, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)]
@@ -302,6 +303,10 @@ class Engine:
     def set_persistent(self, on: bool):
         """Run the small classes of both precisions as one persistent work-queue launch."""
         self._check(lib().hfg_set_persistent(self.h, 1 if on else 0))
+
+    def set_autotune(self, on: bool):
+        """Time the kernel forms of a class on its first large build (default) or run the default forms only."""
+        self._check(lib().hfg_set_autotune(self.h, 1 if on else 0))
 
     def set_gradient_form(self, group_only: bool):
         """Gradient kernels: the lane-group form for every class (True) or the thread form where compiled."""

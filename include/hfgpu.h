@@ -185,6 +185,12 @@ int hfg_set_graph_mode(hfg_engine* engine, int on);
  * rounding (the digestion's atomics sum in a different order). */
 int hfg_set_persistent(hfg_engine* engine, int on);
 
+/* Kernel-form autotuning (no reference counterpart): on (default), the first build that runs a class with at
+ * least 64k surviving quartets and more than one compiled form times the forms on a sample of its list and
+ * keeps the fastest (hfg_kernel_forms reports the picks); off, every class not set by hfg_set_kernel_form
+ * runs its default form, with no timing trials (reproducible launch sequences, e.g. under a profiler). */
+int hfg_set_autotune(hfg_engine* engine, int on);
+
 /* Gradient kernel form (no reference counterpart): 0 (default) runs the thread-per-quartet gradient kernel
  * for the classes whose per-quartet arrays fit in registers ((ss|ss) (ps|ss) (ps|ps) (pp|ss) (ds|ss) in
  * FP64, and (pp|ps) (ds|ps) (dp|ss) as well in FP32) and the lane-group kernel for the others; 1 runs the
