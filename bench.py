@@ -44,6 +44,8 @@ for _p in (REPO, os.path.join(REPO, "hartree-fock_gb300")):
         sys.path.insert(0, _p)
 
 METRIC = "Fock builds/s & SCF time, (H2O)_64/6-31G**: mixed vs FP64 GPU, |ΔE|≤1e-6 Eh"
+# DRAM traffic per mixed build of the ERI class kernels, measured with ncu on the default kernel forms.
+ERI_DRAM_BYTES_PER_BUILD = {"h2o64": 12.52e9}
 WORKLOADS = {
     "h2o64": dict(lattice=(4, 4, 4), basis="6-31G**", name="(H2O)_64 RHF/6-31G** direct Fock build (1600 bf)"),
     "h2o32": dict(lattice=(4, 4, 2), basis="6-31G**", name="(H2O)_32 RHF/6-31G** direct Fock build (800 bf)"),
@@ -249,15 +251,19 @@ class CpuBuild:
         return {"seconds": t, "quartets": int(n), "builds_per_s": 1.0 / t}
 
 
-def cpu_baseline(soa, Z, xyz, Da, target_s: float, total_quartets: int | None = None):
-    """A bounded CPU sample (about target_s seconds of work) for the GPU arm's cpu_baseline object."""
-    cb = CpuBuild(soa, Z, xyz, Da, total_quartets)
-    r = cb.sample(cb.calibrate(target_s), seed=0)
-    return {"value": r["builds_per_s"], "unit": "Fock builds/s", "cores": cb.cores, "kind": "port",
-            "sample": (f"{r['bra_pairs']} of {cb.npairs} ordered bra shell pairs (seeded, {100 * r['fraction']:.3f}% of "
-                       f"the build's loop; {r['quartets']} of {cb.total} surviving quartets) in {r['seconds']:.2f} s "
-                       f"measured; builds/s = sampled fraction / measured seconds"),
-            "build": "oracle/hf_oracle.c with the reference's release flags (Makefile:47, without -march=native/-flto)"}
+def cpu_baseline(workload: str, target_s: float):
+    """The GPU arm's cpu_baseline object: the reference arm of this script run in a child process (one
+    warm-up and one timed sample of about target_s seconds), so that the OpenMP build runs in a process
+    without PyTorch (whose own OpenMP runtime and threads slowed it 3x in the GPU arm's process)."""
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT")}
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--workload", workload,
+           "--steps", "1", "--warmup", "1", "--cpu-seconds", str(target_s / 6.0)]
+    r = subprocess.run(cmd, env=env, capture_output=True, text=True, check=True)
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    cpu = dict(line["cpu_baseline"])
+    cpu["how"] = "child process: bench.py --impl reference --steps 1 --warmup 1 (no PyTorch in the process)"
+    return cpu
 
 
 def reference_arm(args, dist):
@@ -394,9 +400,8 @@ def gpu_arm(args, dist):
     out = None
     if dist.rank == 0:
         cpu = None
-        if not args.no_cpu_baseline:
-            nq = sum(st["quartets_fp64"]) + sum(st["quartets_fp32"])
-            cpu = cpu_baseline(soa, Z, xyz, Da, args.cpu_seconds, total_quartets=nq)
+        if not args.no_cpu_baseline and dist.world == 1:
+            cpu = cpu_baseline(args.workload, args.cpu_seconds)
         out = {
             "metric": METRIC, "value": value, "unit": "Fock builds/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -422,7 +427,13 @@ def gpu_arm(args, dist):
                          "unit": "TFLOP/s (FP64-equivalent: FP32 flops x peak64/peak32, over the kernels' common span)",
                          "frac": ach_mix / peak64 if peak64 else None,
                          "peak_source": "measured FP64 / FP32 FMA loops (hfg_measure_fma_peak) on this GPU",
-                         "traffic": None,
+                         # DRAM bytes (read + write) of the ERI class kernels of one mixed (H2O)_64 build: ncu's
+                         # dram__bytes_read.sum + dram__bytes_write.sum over the jk_class kernels of
+                         # `bench.py --steps 2 --warmup 3 --no-cpu-baseline --no-scf --no-tune`.
+                         "traffic": ERI_DRAM_BYTES_PER_BUILD.get(args.workload),
+                         "traffic_unit": "bytes per build (ERI class kernels, ncu)",
+                         "traffic_gbs": (ERI_DRAM_BYTES_PER_BUILD[args.workload] / (t_mix * 1e-3) / 1e9
+                                         if args.workload in ERI_DRAM_BYTES_PER_BUILD and t_mix > 0 else None),
                          "fp64_kernels_alone": {"achieved": ach64, "peak": peak64, "unit": "TFLOP/s",
                                                 "frac": ach64 / peak64 if peak64 else None,
                                                 "where": "FP64 class kernels of the plain FP64 build"},
