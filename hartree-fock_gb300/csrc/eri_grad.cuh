@@ -62,7 +62,10 @@ template <int LA, int LB, int LC, int LD> struct GradLayout
     // so that the small classes do not leave most of a warp idle; a warp holds 32 / kGroup quartets.
     static constexpr int kWork  = kG > kX ? kG : kX;
     static constexpr int kGroup = kWork <= 16 ? 4 : kWork <= 32 ? 8 : kWork <= 64 ? 16 : 32;
-    static constexpr int kPerGroup = ((kR + kG + kX + kGam + 1) / 2) * 2;
+    // Per-primitive-quartet scalars (P - Q and the scaled Boys values F_0..F_L), computed by the group's
+    // lanes for kGroup primitive quartets at once (one each) instead of by every lane for each.
+    static constexpr int kScal = L + 4, kS = kGroup * kScal;
+    static constexpr int kPerGroup = ((kR + kG + kX + kGam + kS + 1) / 2) * 2;
     static constexpr int kPerWarp  = kPerGroup * (32 / kGroup);
 };
 
@@ -112,6 +115,8 @@ __global__ void __launch_bounds__(32 * kGradWarps)
     Real* Gs    = wbase + 2 * HL;
     Real* Xs    = Gs + W::kG;
     Real* Gam   = Xs + W::kX;
+    Real* Sb    = Gam + W::kGam; // kGroup rows of kScal scalars
+    constexpr int kScal = W::kScal;
     const Real* Dt = static_cast<const Real*>(v.Dt);
     const Real* Da = static_cast<const Real*>(v.Da);
     const Real* Db = static_cast<const Real*>(v.Db);
@@ -140,9 +145,9 @@ __global__ void __launch_bounds__(32 * kGradWarps)
         __syncwarp(gmask);
         Real gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
 
-        // R^0_{tuv} of one primitive quartet into one of the group's two R buffers (levels in parallel over
-        // the group's lanes); returns the buffer that holds it.
-        auto group_R = [&](const Real* rb, const Real* rk) -> const Real*
+        // The scalars of one primitive quartet into a row of the group's buffer: P - Q, then
+        // Fs[n] = pref (-2 rho)^n F_n.  Each lane fills its own row, for a different primitive quartet.
+        auto prim_scalars = [&](const Real* rb, const Real* rk, Real* row)
         {
             const Real p = rb[0], qq = rk[0];
             const Real X = rb[1] - rk[1], Y = rb[2] - rk[2], Z = rb[3] - rk[3];
@@ -152,17 +157,24 @@ __global__ void __launch_bounds__(32 * kGradWarps)
             const Real T    = rho * (X * X + Y * Y + Z * Z);
             Real F[L + 1];
             boys_eval<L, Real>(T, slice, F);
-            Real Fs[L + 1];
-            {
-                const Real m2r = Real(-2) * rho;
-                Real w         = pref;
+            row[0] = X;
+            row[1] = Y;
+            row[2] = Z;
+            const Real m2r = Real(-2) * rho;
+            Real w         = pref;
 #pragma unroll
-                for (int k = 0; k <= L; ++k)
-                {
-                    Fs[k] = w * F[k];
-                    w *= m2r;
-                }
+            for (int k = 0; k <= L; ++k)
+            {
+                row[3 + k] = w * F[k];
+                w *= m2r;
             }
+        };
+        // R^0_{tuv} of one buffered primitive quartet into one of the group's two R buffers (levels in
+        // parallel over the group's lanes); returns the buffer that holds it.
+        auto group_R = [&](const Real* row) -> const Real*
+        {
+            const Real X = row[0], Y = row[1], Z = row[2];
+            const Real* Fs = row + 3;
             Real* src = Rbuf0;
             Real* dst = Rbuf1;
             if (lane == 0)
@@ -208,9 +220,17 @@ __global__ void __launch_bounds__(32 * kGradWarps)
             for (int e = lane; e < HAB1 * NCD; e += GS) Gs[e] = Real(0);
             for (int ik = 0; ik < ket.npp; ++ik)
             {
-                const Real* __restrict__ rk = static_cast<const Real*>(v.pptab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * SK;
+                const int j = ik % GS;
+                if (j == 0)
+                {
+                    // The next GS ket primitives' scalars, one per lane.
+                    if (ik + lane < ket.npp)
+                        prim_scalars(rb, static_cast<const Real*>(v.pptab[PCK]) + static_cast<size_t>(ket.pp_off + ik + lane) * SK,
+                                     Sb + lane * kScal);
+                    __syncwarp(gmask);
+                }
                 const Real* __restrict__ gk = static_cast<const Real*>(v.gtab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * GK;
-                const Real* R = group_R(rb, rk);
+                const Real* R = group_R(Sb + j * kScal);
                 auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
                 for (int e = lane; e < HAB1 * NCD; e += GS)
                 {
@@ -281,9 +301,17 @@ __global__ void __launch_bounds__(32 * kGradWarps)
             for (int e = lane; e < NAB * HCD1; e += GS) Xs[e] = Real(0);
             for (int ib = 0; ib < bra.npp; ++ib)
             {
-                const Real* __restrict__ rb = static_cast<const Real*>(v.pptab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * SB;
+                const int j = ib % GS;
+                if (j == 0)
+                {
+                    // The next GS bra primitives' scalars, one per lane.
+                    if (ib + lane < bra.npp)
+                        prim_scalars(static_cast<const Real*>(v.pptab[PCB]) + static_cast<size_t>(bra.pp_off + ib + lane) * SB, rk,
+                                     Sb + lane * kScal);
+                    __syncwarp(gmask);
+                }
                 const Real* __restrict__ gb = static_cast<const Real*>(v.gtab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * GB;
-                const Real* R = group_R(rb, rk);
+                const Real* R = group_R(Sb + j * kScal);
                 auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
                 for (int e = lane; e < NAB * HCD1; e += GS)
                 {
