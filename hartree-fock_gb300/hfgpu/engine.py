@@ -214,7 +214,7 @@ class Engine:
         Q = np.asfortranarray(Q, dtype=np.float64).ravel(order="F")
         self._check(lib().hfg_set_schwartz(self.h, _dp(Q)))
 
-    def fock(self, dD_tot, dD_alpha, dD_beta=None, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-4,
+    def fock(self, dD_tot, dD_alpha, dD_beta=None, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=2e-4,
              out=None):
         """(J, Ka, Kb or None, stats dict) for host numpy matrices (single molecule: n x n).  `out`: optional
         caller-owned flat float64 host buffers [J, Ka(, Kb)] (e.g. pinned memory) that receive the result."""
@@ -278,7 +278,7 @@ class Engine:
         outs = [o.reshape(n, n, order="F") if o is not None else None for o in outs]
         return outs[0], outs[1], outs[2], st.as_dict()
 
-    def fock_device(self, ptrs: dict, unrestricted=False, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=1e-4):
+    def fock_device(self, ptrs: dict, unrestricted=False, precision=FP64, sthr=1e-10, dthr=1e-10, fp32_cutoff=2e-4):
         """Same on device pointers (ints): keys dD_tot, dD_alpha, dD_beta, J, K_alpha, K_beta."""
         g = lambda k: ptrs.get(k) or None
         req = _Request(1 if unrestricted else 0, precision, 1, sthr, dthr, fp32_cutoff, g("dD_tot"), g("dD_alpha"),
@@ -365,7 +365,7 @@ class Engine:
         return Da, Db
 
     def gradient(self, Z, xyz, Da=None, Db=None, W=None, unrestricted=False, sthr=1e-10, dthr=1e-10,
-                 precision=FP64, fp32_cutoff=1e-4):
+                 precision=FP64, fp32_cutoff=2e-4):
         """Nuclear gradient (natom x 3, Eh/bohr) and the two-electron device time in ms.  With Da None the
         densities of this engine's last scf() are used (the backward half of scf()).  precision MIXED runs
         the small-bound quartets' derivative integrals in FP32."""
@@ -430,7 +430,7 @@ def measure_dmma_peak(device: int = 0) -> float:
     return t.value
 
 
-def run_input(text: str, precision: int = FP64, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0,
+def run_input(text: str, precision: int = FP64, fp32_cutoff: float = 2e-4, full_rebuild_every: int = 0,
               basis_dir: str | None = None, device: int = 0, graphs: bool = False, input_frame: bool = False):
     """Runs a reference-format input end to end: parse, pack the basis, GPU direct SCF (graphs: replay
     the Fock builds of the SCF iterations as CUDA graphs).

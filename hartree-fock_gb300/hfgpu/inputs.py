@@ -97,7 +97,7 @@ def check_supported(job: JobInput, input_frame: bool = False) -> None:
                          "densities and gradients in the input frame)")
 
 
-def scf_options(job: JobInput, precision: int = 0, fp32_cutoff: float = 1e-4, full_rebuild_every: int = 0) -> dict:
+def scf_options(job: JobInput, precision: int = 0, fp32_cutoff: float = 2e-4, full_rebuild_every: int = 0) -> dict:
     """The hfg_scf_options fields for a parsed job, with the reference's defaults."""
     s = job.scf
     max_iter = s.get("max_iter", 30)

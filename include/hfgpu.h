@@ -263,7 +263,7 @@ typedef struct hfg_scf_options
     double schwartz_threshold; /* SCHWARTZ_THRESH (1e-10) */
     double density_threshold;  /* DENSITY_THRESH (1e-10) */
     int precision;             /* HFG_PRECISION_FP64 / HFG_PRECISION_MIXED */
-    double fp32_cutoff;        /* FP32 cutoff of the mixed mode (1e-4) */
+    double fp32_cutoff;        /* FP32 cutoff of the mixed mode (2e-4) */
     int full_rebuild_every;    /* 0: incremental builds as the reference; k > 0: full build every k iterations */
     int verbose;               /* print the iteration table to stdout */
     int graph_iterations;      /* 1: every SCF iteration after the first replays CUDA graphs captured once: the Fock

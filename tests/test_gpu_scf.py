@@ -1,6 +1,6 @@
 """End-to-end direct SCF with the GPU Fock build against the reference's converged energies
 (golden fixtures from SCF::run, converged to ENERGY_TOL 1e-10): |E_gpu - E_ref| <= 1e-9 Eh on the FP64
-path; the mixed FP32/FP64 path, at the shipped default FP32 cutoff (1e-4), within 1e-6 Eh of the FP64 GPU energy."""
+path; the mixed FP32/FP64 path, at the shipped default FP32 cutoff (2e-4), within 1e-6 Eh of the FP64 GPU energy."""
 import numpy as np
 import pytest
 
@@ -28,7 +28,7 @@ def test_gpu_scf_mixed_energy_close_to_fp64(name):
 
     g = load_golden(name)
     r64, _, _, _ = run_input(str(g["input_text"]))
-    r32, _, _, _ = run_input(str(g["input_text"]), precision=1)  # the default fp32_cutoff, 1e-4
+    r32, _, _, _ = run_input(str(g["input_text"]), precision=1)  # the default fp32_cutoff, 2e-4
     assert r32["converged"] == 1
     assert abs(r32["e_total"] - r64["e_total"]) <= 1e-6
 
