@@ -54,3 +54,18 @@ def test_reference_arm_under_torchrun_two_ranks():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_gpu_arm_cpu_baseline_runs_in_a_clean_child(monkeypatch):
+    """The GPU arm's cpu_baseline is the reference arm run as a child process: it must not inherit the
+    torchrun rendezvous variables (the child would try to join the process group) and it reports the
+    measured sample."""
+    import bench
+
+    for k, v in (("RANK", "0"), ("WORLD_SIZE", "2"), ("LOCAL_RANK", "0"), ("MASTER_ADDR", "127.0.0.1"),
+                 ("MASTER_PORT", str(_free_port()))):
+        monkeypatch.setenv(k, v)
+    cpu = bench.cpu_baseline("h2o16", 1.0)
+    assert cpu["kind"] == "port" and cpu["unit"] == "Fock builds/s"
+    assert cpu["value"] > 0 and cpu["cores"] >= 1
+    assert "measured" in cpu["sample"] and "child process" in cpu["how"]

@@ -186,3 +186,26 @@ def test_gpu_persistent_queue_matches_reference(name):
         Jg = outs[0].cpu().numpy().reshape(n, n, order="F")
         Kg = outs[1].cpu().numpy().reshape(n, n, order="F")
         assert np.max(np.abs((Jg - Kg) - g["Fa"])) <= 1e-10
+
+
+def test_gpu_autotune_off_runs_default_forms():
+    """With autotuning off no class is timed (ms_tune 0, no timed picks recorded) and every class runs its
+    default form; the build agrees with the autotuned one to rounding."""
+    from hfgpu import basis, workloads
+    from hfgpu.engine import Engine
+
+    Z, xyz = workloads.water_lattice(4, 2, 2, spacing=5.5, seed=0, jitter=0.2)
+    soa = basis.pack("6-31G**", Z, xyz)
+    e0 = Engine(soa)
+    Da, _ = e0.core_guess(Z, xyz, 0, 1)
+    J0, K0, _, _ = e0.fock(2 * Da, Da, precision=1)
+    e1 = Engine(soa)
+    e1.set_autotune(False)
+    for _ in range(2):
+        J1, K1, _, st = e1.fock(2 * Da, Da, precision=1)
+        assert st["ms_tune"] == 0.0
+    for fp32 in (False, True):
+        forms, avail = e1.kernel_forms(fp32=fp32)
+        # 0: untuned (the default form ran); a class with a single compiled form reports that form.
+        assert all(f == 0 or (m & (m - 1)) == 0 for f, m in zip(forms, avail))
+    assert np.max(np.abs(J1 - J0)) <= 1e-10 and np.max(np.abs(K1 - K0)) <= 1e-10
