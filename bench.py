@@ -45,7 +45,7 @@ for _p in (REPO, os.path.join(REPO, "hartree-fock_gb300")):
 
 METRIC = "Fock builds/s & SCF time, (H2O)_64/6-31G**: mixed vs FP64 GPU, |ΔE|≤1e-6 Eh"
 # DRAM traffic per mixed build of the ERI class kernels, measured with ncu on the default kernel forms.
-ERI_DRAM_BYTES_PER_BUILD = {"h2o64": 12.52e9}
+ERI_DRAM_BYTES_PER_BUILD = {"h2o64": 12.45e9}
 WORKLOADS = {
     "h2o64": dict(lattice=(4, 4, 4), basis="6-31G**", name="(H2O)_64 RHF/6-31G** direct Fock build (1600 bf)"),
     "h2o32": dict(lattice=(4, 4, 2), basis="6-31G**", name="(H2O)_32 RHF/6-31G** direct Fock build (800 bf)"),
