@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                       const Real* __restrict__ boys_slice, const WarpTables* __restrict__ tabs)
 {
     using W = GradLayout<LA, LB, LC, LD>;
-    constexpr int NA = W::NA, NB = W::NB, NC = W::NC, ND = W::ND, NAB = W::NAB, NCD = W::NCD;
+    constexpr int NB = W::NB, ND = W::ND, NAB = W::NAB, NCD = W::NCD;
     constexpr int LAB = W::LAB, LCD = W::LCD, L = W::L, HAB1 = W::HAB1, HCD1 = W::HCD1, HL = W::HL;
     constexpr int SB = pp_stride(LA, LB), SK = pp_stride(LC, LD);
     constexpr int GB = g_stride(LA, LB), GK = g_stride(LC, LD);
@@ -229,7 +229,9 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                                      Sb + lane * kScal);
                     __syncwarp(gmask);
                 }
-                const Real* __restrict__ gk = static_cast<const Real*>(v.gtab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * GK;
+                // The ket's 3-D Hermite coefficients E^{kl}_{tau nu phi} from its forward record (one DFMA per
+                // term; products of the 1-D tables would cost a DMUL more on the FP64 pipe).
+                const Real* __restrict__ rk = static_cast<const Real*>(v.pptab[PCK]) + static_cast<size_t>(ket.pp_off + ik) * SK;
                 const Real* R = group_R(Sb + j * kScal);
                 auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
                 for (int e = lane; e < HAB1 * NCD; e += GS)
@@ -237,23 +239,17 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     const int h = e / NCD, kl = e % NCD;
                     const int tuv = tabs->htuv[LAB + 1][h];
                     const int t = tuv & 255, u = (tuv >> 8) & 255, w_ = tuv >> 16;
-                    const int k = kl / ND, l = kl % ND;
-                    const int kx = cart_exp(LC, k, 0), ky = cart_exp(LC, k, 1), kz = cart_exp(LC, k, 2);
-                    const int lx = cart_exp(LD, l, 0), ly = cart_exp(LD, l, 1), lz = cart_exp(LD, l, 2);
-                    const Real* Ex = gk + 2;
-                    const Real* Ey = Ex + G1K;
-                    const Real* Ez = Ey + G1K;
-                    Real s = Real(0);
-                    for (int ph = 0; ph <= kz + lz; ++ph)
-                        for (int nu = 0; nu <= ky + ly; ++nu)
-                        {
-                            const Real eyz = e1(Ey, LD, LCD, ky, ly, nu) * e1(Ez, LD, LCD, kz, lz, ph);
-                            for (int ta = 0; ta <= kx + lx; ++ta)
+                    const int4 g3 = tabs->e3[PCK][kl]; // 1-D range lengths, offset in the record
+                    const Real* E3 = rk + g3.w;
+                    Real s   = Real(0);
+                    int idx  = 0;
+                    for (int ph = 0; ph < g3.z; ++ph)
+                        for (int nu = 0; nu < g3.y; ++nu)
+                            for (int ta = 0; ta < g3.x; ++ta, ++idx)
                             {
-                                const Real ek = eyz * e1(Ex, LD, LCD, kx, lx, ta);
+                                const Real ek = (LCD == 0) ? Real(1) : E3[idx];
                                 s = fma(((ta + nu + ph) & 1) ? -ek : ek, Ridx(t + ta, u + nu, w_ + ph), s);
                             }
-                        }
                     Gs[e] += s;
                 }
                 __syncwarp(gmask); // G read R; the next primitive quartet overwrites the R buffers
@@ -310,7 +306,8 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                                      Sb + lane * kScal);
                     __syncwarp(gmask);
                 }
-                const Real* __restrict__ gb = static_cast<const Real*>(v.gtab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * GB;
+                // The bra's 3-D Hermite coefficients from its forward record, as for the ket in the first pass.
+                const Real* __restrict__ rb = static_cast<const Real*>(v.pptab[PCB]) + static_cast<size_t>(bra.pp_off + ib) * SB;
                 const Real* R = group_R(Sb + j * kScal);
                 auto Ridx = [&](int t, int u, int w_) { return R[tabs->cube[L][(t * S + u) * S + w_]]; };
                 for (int e = lane; e < NAB * HCD1; e += GS)
@@ -318,20 +315,14 @@ __global__ void __launch_bounds__(32 * kGradWarps)
                     const int ij = e / HCD1, h = e % HCD1;
                     const int tuv = tabs->htuv[LCD + 1][h];
                     const int ta = tuv & 255, nu = (tuv >> 8) & 255, ph = tuv >> 16;
-                    const int i = ij / NB, j = ij % NB;
-                    const int ix = cart_exp(LA, i, 0), iy = cart_exp(LA, i, 1), iz = cart_exp(LA, i, 2);
-                    const int jx = cart_exp(LB, j, 0), jy = cart_exp(LB, j, 1), jz = cart_exp(LB, j, 2);
-                    const Real* Ex = gb + 2;
-                    const Real* Ey = Ex + G1B;
-                    const Real* Ez = Ey + G1B;
-                    Real s = Real(0);
-                    for (int w_ = 0; w_ <= iz + jz; ++w_)
-                        for (int u = 0; u <= iy + jy; ++u)
-                        {
-                            const Real eyz = e1(Ey, LB, LAB, iy, jy, u) * e1(Ez, LB, LAB, iz, jz, w_);
-                            for (int t = 0; t <= ix + jx; ++t)
-                                s += eyz * e1(Ex, LB, LAB, ix, jx, t) * Ridx(t + ta, u + nu, w_ + ph);
-                        }
+                    const int4 g3 = tabs->e3[PCB][ij];
+                    const Real* E3 = rb + g3.w;
+                    Real s  = Real(0);
+                    int idx = 0;
+                    for (int w_ = 0; w_ < g3.z; ++w_)
+                        for (int u = 0; u < g3.y; ++u)
+                            for (int t = 0; t < g3.x; ++t, ++idx)
+                                s = fma((LAB == 0) ? Real(1) : E3[idx], Ridx(t + ta, u + nu, w_ + ph), s);
                     Xs[e] += s;
                 }
                 __syncwarp(gmask);
